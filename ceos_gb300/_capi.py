@@ -1,0 +1,126 @@
+"""ctypes binding of the C ABI in include/ceos_gb300.h.
+
+The shared library is built in-tree by ``ceos_gb300.build``. There is no CPU
+fallback: if the library is missing or no CUDA device is visible, the calls
+raise instead of silently computing something else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libceos_gb300.so")
+
+OK = 0
+ERR_ARG = -1
+ERR_NOT_BUILT = -2
+ERR_PROBED_POINTS = -3
+ERR_PROBED_VECTORS = -4
+ERR_UPDATE_DEL = -5
+ERR_UPDATE_TOPM = -6
+ERR_CUDA = -7
+ERR_NO_DEVICE = -8
+ERR_UNSUPPORTED = -9
+ERR_DEVICE_LIMIT = -10
+
+ALGO_DENSE, ALGO_COCEOS, ALGO_HASH = 0, 1, 2
+PRECISION_FP32, PRECISION_SPLIT_BF16 = 0, 1
+
+F32P = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+I32P = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+U8P = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+VP = C.c_void_p
+IP = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes); every entry point declared in include/ceos_gb300.h
+SIGNATURES = {
+    "ceos_abi_version": (C.c_int, []),
+    "ceos_last_error": (C.c_char_p, []),
+    "ceos_device_count": (C.c_int, []),
+    "ceos_set_log_level": (None, [C.c_int]),
+    "ceos_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(VP)]),
+    "ceos_destroy": (None, [VP]),
+    "ceos_set_index_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "ceos_get_index_param": (C.c_int, [VP, IP, IP, IP, IP, IP, IP]),
+    "ceos_set_threads": (C.c_int, [VP, C.c_int]),
+    "ceos_clear": (C.c_int, [VP]),
+    "ceos_set_query_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
+    "ceos_get_query_param": (C.c_int, [VP, IP, IP, IP]),
+    "ceos_set_centering": (C.c_int, [VP, C.c_int]),
+    "ceos_get_centering": (C.c_int, [VP, IP]),
+    "ceos_set_precision": (C.c_int, [VP, C.c_int]),
+    "ceos_build": (C.c_int, [VP, F32P]),
+    "ceos_search": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
+    "ceos_build_coceos_est": (C.c_int, [VP, F32P]),
+    "ceos_search_coceos_est": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
+    "ceos_build_ceos_hash": (C.c_int, [VP, F32P]),
+    "ceos_search_ceos_hash": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
+    "ceos_search_device": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, VP, VP, VP]),
+    "ceos_get_buckets": (C.c_int, [VP, I32P, F32P]),
+    "ceos_get_projections": (C.c_int, [VP, F32P]),
+    "ceos_get_sign_bits": (C.c_int, [VP, U8P]),
+    "ceos_last_timings": (C.c_int, [VP, F32P, C.c_int]),
+    "ceos_timing_name": (C.c_char_p, [VP, C.c_int]),
+    "ceos_stream_create": (C.c_int, [C.c_int, C.POINTER(VP)]),
+    "ceos_stream_destroy": (None, [VP]),
+    "ceos_stream_set_index_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "ceos_stream_set_threads": (C.c_int, [VP, C.c_int]),
+    "ceos_stream_clear": (C.c_int, [VP]),
+    "ceos_stream_set_query_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
+    "ceos_stream_get_query_param": (C.c_int, [VP, IP, IP, IP]),
+    "ceos_stream_build": (C.c_int, [VP, F32P, C.c_int]),
+    "ceos_stream_update": (C.c_int, [VP, VP, C.c_int, C.c_int]),
+    "ceos_stream_estimate_search": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
+    "ceos_stream_hash_search": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
+    "ceos_stream_size": (C.c_int, [VP, IP]),
+    "ceos_stream_get_buckets": (C.c_int, [VP, I32P, F32P]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class CEOsError(RuntimeError):
+    """A CUDA or device-limit failure inside the library."""
+
+
+def lib():
+    """Load the in-tree shared library (building it first if it is absent)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                from . import build as _build
+
+                _build.build()
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            if L.ceos_abi_version() != 1:
+                raise CEOsError("libceos_gb300.so ABI version mismatch")
+            _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().ceos_last_error().decode(errors="replace")
+
+
+def check(status: int) -> None:
+    """Translate a C ABI status into the Python exception the reference's
+    error paths correspond to (they print and exit(1))."""
+    if status == OK:
+        return
+    msg = last_error()
+    if status in (ERR_ARG, ERR_PROBED_POINTS, ERR_PROBED_VECTORS, ERR_UPDATE_DEL, ERR_UPDATE_TOPM,
+                  ERR_UNSUPPORTED):
+        raise ValueError(msg)
+    if status == ERR_NOT_BUILT:
+        raise RuntimeError(msg)
+    raise CEOsError(f"[{status}] {msg}")

@@ -1,0 +1,160 @@
+// Bit-exact seeded sign-flip + Walsh-Hadamard projection on the GPU.
+//
+// The reference computes, for every row x (zero-padded to F = 2^L) and every
+// repeat r, three rounds of {v_j *= +-1 ; v = FWHT(v)} and keeps the first D
+// outputs (src/CEOs.cpp:58-88, query side :143-161). Its FWHT is FFHT's
+// fht_float (src/fht_avx.c:10081), which is bit-identical to the radix-2
+// butterfly applied in ASCENDING stage order: stage s maps every pair of
+// indices (j, j + 2^s) with bit s of j clear to (a + b, a - b).
+//
+// GPU form. One warp owns V vectors (V = 1 for F = 1024). The vector lives in
+// shared memory between "phases"; a phase applies a contiguous run of stages
+// [o, o + b) entirely in registers: a lane loads a "line" of E = 2^b elements
+// whose indices differ only in bits [o, o + b), runs the b butterfly stages
+// on them in ascending order, and stores them back. The stage order, and
+// therefore every rounding, is the reference's. Phase 0 (bits [0, b0)) reads
+// contiguous chunks and applies the sign flip of the round while loading, as
+// an XOR of the float sign bit (identical to multiplying by +-1.0f, -0.0
+// included). The last phase of the last round leaves the outputs in
+// registers, where the callers consume them (store, or compare against
+// selection thresholds).
+//
+// Shared memory is padded by 4 floats every 32 so that phase 0 (lane stride of
+// E floats) and the last phase (consecutive lanes on consecutive indices) are
+// both free of bank conflicts.
+#pragma once
+
+#include "common.cuh"
+
+namespace ceos {
+
+template <int L>
+struct FwhtCfg {
+  static constexpr int F = 1 << L;
+  static constexpr int P = (L + 4) / 5;  // phases of at most 5 stages
+  __host__ __device__ static constexpr int bits(int p) { return L / P + (p < L % P ? 1 : 0); }
+  __host__ __device__ static constexpr int off(int p) { return p == 0 ? 0 : off(p - 1) + bits(p - 1); }
+  __host__ __device__ static constexpr int E(int p) { return 1 << bits(p); }
+  static constexpr int Emax = 1 << (L / P + (L % P ? 1 : 0));
+  static constexpr int V = (32 * Emax / F) > 1 ? (32 * Emax / F) : 1;  // vectors per warp
+  __host__ __device__ static constexpr int tasks(int p) { return V * F / (32 * E(p)); }    // lines per lane
+  static constexpr int Fpad = F + (F >= 32 ? (F / 32) * 4 : 0);
+  // vector stride in smem; an extra 16 floats de-phases the banks of the V
+  // vectors that share a warp
+  static constexpr int Vstride = Fpad + (V > 1 ? 16 : 0);
+  static constexpr int words = F >= 32 ? F / 32 : 1;  // sign words per round
+};
+
+CEOS_DEV int padj(int j) { return j + ((j >> 5) << 2); }
+
+// Index of element e of line `line` in a phase covering bits [o, o + b).
+CEOS_DEV int line_elem(int line, int e, int o, int b) {
+  const int low = line & ((1 << o) - 1);
+  const int high = line >> o;
+  return low | (e << o) | (high << (o + b));
+}
+
+// Butterfly stages [0, b) of a register line (stage s pairs e and e + 2^s).
+template <int B>
+CEOS_DEV void reg_stages(float (&v)[1 << B]) {
+#pragma unroll
+  for (int s = 0; s < B; ++s) {
+    const int h = 1 << s;
+#pragma unroll
+    for (int e = 0; e < (1 << B); ++e) {
+      if ((e & h) == 0) {
+        const float a = v[e], c = v[e + h];
+        v[e] = a + c;
+        v[e + h] = a - c;
+      }
+    }
+  }
+}
+
+// Phase p >= 1 of a round: bits [off(p), off(p) + bits(p)) in registers.
+template <int L, int p, bool KEEP_LAST>
+CEOS_DEV void fwht_phase(float* dst, int lane, float (*out)[FwhtCfg<L>::Emax]) {
+  using Cfg = FwhtCfg<L>;
+  constexpr int o = Cfg::off(p);
+  constexpr int B = Cfg::bits(p);
+  constexpr int E = 1 << B;
+  constexpr int lines = Cfg::F / E;
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < Cfg::tasks(p); ++t) {
+    const int task = lane + 32 * t;
+    const int vec = task / lines;
+    const int line = task % lines;
+    float* d = dst + vec * Cfg::Vstride;
+    float v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = d[padj(line_elem(line, e, o, B))];
+    reg_stages<B>(v);
+    if (KEEP_LAST && p == Cfg::P - 1) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) out[t][e] = v[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) d[padj(line_elem(line, e, o, B))] = v[e];
+    }
+  }
+  if constexpr (p + 1 < Cfg::P) fwht_phase<L, p + 1, KEEP_LAST>(dst, lane, out);
+}
+
+// One full round (sign flip + FWHT) on the warp's V vectors.
+//  src: smem base the round reads from (V vectors, stride Vstride)
+//  dst: smem base it writes to (may equal src)
+//  sw : 32-bit sign words of this round (bit j set => multiply by +1)
+// If KEEP_LAST, the last phase's register lines are left in `out`
+// (tasks(P-1) lines of E(P-1) floats) and are NOT stored to dst.
+template <int L, bool KEEP_LAST>
+CEOS_DEV void fwht_round(const float* src, float* dst, const uint32_t* sw, int lane,
+                         float (*out)[FwhtCfg<L>::Emax]) {
+  using Cfg = FwhtCfg<L>;
+  constexpr int B = Cfg::bits(0);
+  constexpr int E = 1 << B;
+  constexpr int lines0 = Cfg::F / E;
+#pragma unroll
+  for (int t = 0; t < Cfg::tasks(0); ++t) {
+    const int task = lane + 32 * t;
+    const int vec = task / lines0;
+    const int line = task % lines0;
+    const int j0 = line * E;
+    const float* s = src + vec * Cfg::Vstride;
+    float* d = dst + vec * Cfg::Vstride;
+    const uint32_t word = sw[j0 >> 5] >> (j0 & 31);
+    float v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const uint32_t flip = ((word >> e) & 1u) ? 0u : 0x80000000u;
+      v[e] = __uint_as_float(__float_as_uint(s[padj(j0 + e)]) ^ flip);
+    }
+    reg_stages<B>(v);
+    if (KEEP_LAST && Cfg::P == 1) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) out[t][e] = v[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) d[padj(j0 + e)] = v[e];
+    }
+  }
+  if constexpr (Cfg::P > 1) fwht_phase<L, 1, KEEP_LAST>(dst, lane, out);
+  __syncwarp();
+}
+
+// Map (task t of the last phase, register e) to the element index j and the
+// vector slot within the warp.
+template <int L>
+CEOS_DEV void last_phase_index(int lane, int t, int e, int& vec, int& j) {
+  using Cfg = FwhtCfg<L>;
+  constexpr int p = Cfg::P - 1;
+  const int o = Cfg::off(p);
+  const int B = Cfg::bits(p);
+  const int lines = Cfg::F / (1 << B);
+  const int task = lane + 32 * t;
+  vec = task / lines;
+  const int line = task % lines;
+  j = line_elem(line, e, o, B);
+}
+
+}  // namespace ceos

@@ -1,0 +1,90 @@
+// Launch interface between the host layer (capi.cu) and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ceos {
+
+enum ProjMode { PROJ_ROWS = 0, PROJ_COLS = 1, PROJ_EMIT = 2 };
+
+struct ProjArgs {
+  // input rows: row `i` of the work list is X[((row_map ? row_map[i] : i) + head) mod cap_rows]
+  const float* X = nullptr;
+  long ldx = 0;
+  const long* row_map = nullptr;
+  long n_rows = 0;
+  long head = 0;
+  long cap_rows = 0;
+  int d = 0, D = 0, R = 0;
+  const uint32_t* signs = nullptr;  // [R][3][max(F/32,1)] words, bit j set => +1
+  // PROJ_ROWS: out[row * R*D + col]; PROJ_COLS: out[slot * ld_out + row]
+  float* out = nullptr;
+  long ld_out = 0;
+  const int* col_slot = nullptr;  // PROJ_COLS: column -> output slot (-1 = skip); null = identity
+  // PROJ_EMIT
+  const uint32_t* th = nullptr;  // [C][2] key thresholds (close: fkey(v), far: fkey(-v))
+  unsigned* cnt = nullptr;       // [C][2] candidate counters
+  uint64_t* cand = nullptr;      // [C][2][cap] packed keys
+  int cap = 0;
+  long id_base = 0;
+  const unsigned char* col_active = nullptr;  // optional per-column enable
+};
+
+cudaError_t launch_project(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st);
+
+// ---- selection (select.cu) ----
+// Per column: u32 thresholds so that about `rank` sample values pass each end.
+cudaError_t launch_sample_thresholds(const float* samp, long S, int C, int rank, uint32_t* th,
+                                     cudaStream_t st);
+// Per column end: top-m of the emitted candidates -> buckets; flags failures.
+cudaError_t launch_finish_buckets(const uint64_t* cand, const unsigned* cnt, int cap, int C, int m,
+                                  int* bids, float* bvals, unsigned* fail, cudaStream_t st);
+// Exact top-m of dumped full columns (fallback): vals [slots][ld] -> buckets of col_of_slot.
+cudaError_t launch_exact_buckets(const float* vals, long n, long ld, int n_slots,
+                                 const int* col_of_slot, const unsigned* fail, int m, int* bids,
+                                 float* bvals, cudaStream_t st);
+
+// ---- queries (query.cu) ----
+struct QueryArgs {
+  const float* Q = nullptr;  // [nq][ldx] (zero padded) device queries
+  const float* qproj = nullptr;  // [nq][C]
+  int nq = 0, d = 0, ldx = 0, C = 0;
+  int s = 0, p = 0, m = 0, c = 0, k = 0;
+  const float* X = nullptr;  // ring of rows, stride ldx
+  long head = 0, cap_rows = 0;
+  long n_points = 0;
+  const int* bids = nullptr;    // [C][2][m]
+  const float* bvals = nullptr; // [C][2][m]
+  const float* P = nullptr;     // dense CEOs-Est projections [C][n]
+  int* out_ids = nullptr;
+  float* out_d = nullptr;
+  // hash table (estimate / union), in shared memory when table_in_smem
+  int table_cap = 0;
+  int table_in_smem = 0;
+  uint64_t* gtable = nullptr;   // [grid][table_cap] workspace when not in smem
+  // dense path
+  const int* probes = nullptr;  // [nq][s] tags in pop order
+  float* est = nullptr;         // [nq][n]
+  int* probes_out = nullptr;
+  uint64_t* gkeys = nullptr;    // [grid][...] rerank workspace (hash union)
+  int gkeys_cap = 0;
+};
+
+enum QueryMode { Q_ESTIMATE = 0, Q_UNION = 1 };
+
+cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem, cudaStream_t st);
+size_t query_buckets_smem(const QueryArgs& a, int mode);
+int query_buckets_blocks_per_sm(int mode, size_t smem);
+cudaError_t launch_probe_select(const QueryArgs& a, cudaStream_t st);
+cudaError_t launch_dense_estimate(const QueryArgs& a, int q0, int nq_chunk, cudaStream_t st);
+cudaError_t launch_dense_select_rerank(const QueryArgs& a, int q0, int nq_chunk, cudaStream_t st);
+
+// ---- streaming (stream.cu) ----
+cudaError_t launch_stream_merge(int C, int m, const float* newP, long b, long cur, int n_del,
+                                int* bids, float* bvals, cudaStream_t st);
+
+// ---- misc ----
+cudaError_t launch_pad_rows(const float* src, long n, int d, float* dst, int ldx, cudaStream_t st);
+
+}  // namespace ceos

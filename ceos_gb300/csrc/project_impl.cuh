@@ -1,0 +1,144 @@
+// Kernel body and launcher of the projection kernels; instantiated per
+// log2(fhtDim) in project_l*.cu so the instantiations compile in parallel.
+#pragma once
+// Projection kernels: the reference's per-row projection block
+// (src/CEOs.cpp:58-88, :343-372, :746-775; src/streamCEOs.cpp:55-86,
+// :229-259) and its query twin (src/CEOs.cpp:143-161, :495-513, :895-913).
+//
+// One kernel body, three consumers of the projected values:
+//   ROWS : row-major [rows][R*D]            (query projections)
+//   COLS : column-major [slot][ld]          (dense CEOs-Est index; sample and
+//                                            fallback dumps of chosen columns)
+//   EMIT : no projection matrix at all. Each value is compared against the
+//          per-column selection thresholds of the bucket build and, when it
+//          can still be among the column's top-m (close end) or bottom-m
+//          (far end), its packed (value, id) key is appended to that column
+//          end's candidate list. This fuses the projection with the first
+//          pass of the two-ended top-m selection (src/CEOs.cpp:377-432), so
+//          the n x (R*D) projection matrix never travels to HBM.
+#include "kernels.h"
+#include "fwht.cuh"
+
+namespace ceos {
+
+// Work split: each warp processes V rows (V vectors) at a time, all R
+// repeats, grid-striding over row groups.
+template <int L, int MODE>
+__global__ void __launch_bounds__(256) k_project(ProjArgs a) {
+  using Cfg = FwhtCfg<L>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int words = Cfg::words;
+  uint32_t* s_signs = reinterpret_cast<uint32_t*>(smem_raw);
+  const int n_sign_words = a.R * 3 * words;
+  float* s_vec = reinterpret_cast<float*>(smem_raw + ((n_sign_words * 4 + 15) & ~15));
+
+  for (int i = threadIdx.x; i < n_sign_words; i += blockDim.x) s_signs[i] = a.signs[i];
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int warps_per_block = blockDim.x >> 5;
+  float* xbuf = s_vec + (size_t)warp * 2 * Cfg::V * Cfg::Vstride;
+  float* wbuf = xbuf + Cfg::V * Cfg::Vstride;
+  const int C = a.R * a.D;
+
+  const long n_groups = (a.n_rows + Cfg::V - 1) / Cfg::V;
+  for (long g = (long)blockIdx.x * warps_per_block + warp; g < n_groups;
+       g += (long)gridDim.x * warps_per_block) {
+    const long row0 = g * Cfg::V;
+    // ---- load V rows (zero padded to F) ----
+    for (int idx = lane; idx < Cfg::V * Cfg::F; idx += 32) {
+      const int v = idx / Cfg::F;
+      const int j = idx % Cfg::F;
+      const long row = row0 + v;
+      float x = 0.0f;
+      if (row < a.n_rows && j < a.d) {
+        long src = a.row_map ? a.row_map[row] : row;
+        src += a.head;
+        if (src >= a.cap_rows) src -= a.cap_rows;
+        x = a.X[src * a.ldx + j];
+      }
+      xbuf[v * Cfg::Vstride + padj(j)] = x;
+    }
+    __syncwarp();
+    for (int r = 0; r < a.R; ++r) {
+      float out[Cfg::tasks(Cfg::P - 1)][Cfg::Emax];
+      const uint32_t* sw = s_signs + (size_t)r * 3 * words;
+      fwht_round<L, false>(xbuf, wbuf, sw, lane, nullptr);
+      fwht_round<L, false>(wbuf, wbuf, sw + words, lane, nullptr);
+      fwht_round<L, true>(wbuf, wbuf, sw + 2 * words, lane, out);
+      constexpr int B = Cfg::bits(Cfg::P - 1);
+#pragma unroll
+      for (int t = 0; t < Cfg::tasks(Cfg::P - 1); ++t) {
+#pragma unroll
+        for (int e = 0; e < (1 << B); ++e) {
+          int vec, j;
+          last_phase_index<L>(lane, t, e, vec, j);
+          const long row = row0 + vec;
+          if (j >= a.D || row >= a.n_rows) continue;
+          const float v = out[t][e];
+          const int col = r * a.D + j;
+          if constexpr (MODE == PROJ_ROWS) {
+            a.out[row * (long)C + col] = v;
+          } else if constexpr (MODE == PROJ_COLS) {
+            const int slot = a.col_slot ? a.col_slot[col] : col;
+            if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v;
+          } else {  // PROJ_EMIT
+            if (a.col_active && !a.col_active[col]) continue;
+            const uint2 th = reinterpret_cast<const uint2*>(a.th)[col];
+            const long id = a.id_base + (a.row_map ? a.row_map[row] : row);
+            if (fkey(v) >= th.x) {
+              const unsigned pos = atomicAdd(&a.cnt[2 * col], 1u);
+              if (pos < (unsigned)a.cap) a.cand[((long)2 * col) * a.cap + pos] = pack_key(v, (int)id);
+            }
+            if (fkey(-v) >= th.y) {
+              const unsigned pos = atomicAdd(&a.cnt[2 * col + 1], 1u);
+              if (pos < (unsigned)a.cap)
+                a.cand[((long)2 * col + 1) * a.cap + pos] = pack_key(-v, (int)id);
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+template <int L>
+static size_t proj_smem(int R) {
+  using Cfg = FwhtCfg<L>;
+  size_t sw = ((size_t)R * 3 * Cfg::words * 4 + 15) & ~(size_t)15;
+  return sw + (size_t)8 * 2 * Cfg::V * Cfg::Vstride * sizeof(float);
+}
+
+template <int L, int MODE>
+cudaError_t launch_L(const ProjArgs& a, int num_sms, cudaStream_t st) {
+  const size_t smem = proj_smem<L>(a.R);
+  cudaError_t e = cudaFuncSetAttribute(k_project<L, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project<L, MODE>, 256, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  using Cfg = FwhtCfg<L>;
+  const long groups = (a.n_rows + Cfg::V - 1) / Cfg::V;
+  long blocks = (groups + 7) / 8;
+  const long max_blocks = (long)num_sms * per_sm;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks < 1) blocks = 1;
+  k_project<L, MODE><<<(unsigned)blocks, 256, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int L>
+cudaError_t launch_project_L(const ProjArgs& a, int mode, int num_sms, cudaStream_t st) {
+  switch (mode) {
+    case PROJ_ROWS: return launch_L<L, PROJ_ROWS>(a, num_sms, st);
+    case PROJ_COLS: return launch_L<L, PROJ_COLS>(a, num_sms, st);
+    case PROJ_EMIT: return launch_L<L, PROJ_EMIT>(a, num_sms, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace ceos

@@ -1,0 +1,6 @@
+// Projection kernel instantiations for log2(fhtDim) in {10}.
+#include "project_impl.cuh"
+
+namespace ceos {
+template cudaError_t launch_project_L<10>(const ProjArgs&, int, int, cudaStream_t);
+}  // namespace ceos

@@ -1,0 +1,171 @@
+/*
+ * ceos_gb300.h - C ABI of the GB300 (sm_103a) CEOs / coCEOs / streamCEOs
+ * maximum-inner-product-search index.
+ *
+ * Every entry point is a plain C function over plain pointers and sizes.
+ * Host-buffer calls copy their inputs to device memory owned by the index and
+ * copy results back; the *_device calls take device pointers and a
+ * cudaStream_t (passed as void*, NULL = the index's own stream).
+ *
+ * Each declaration names the reference interface it replaces (NinhPham/CEOs,
+ * paths relative to that project). The reference binds its classes to Python
+ * through pybind11 in python/python_wrapper.cpp; the same methods map onto
+ * these functions one to one (see INTEGRATION.md for the binding).
+ *
+ * Status codes: every int-returning call returns CEOS_OK (0) or a negative
+ * CEOS_ERR_* code; ceos_last_error() gives the message of the calling
+ * thread's last failure. The reference prints to stderr and calls exit(1) on
+ * the same conditions (src/CEOs.cpp:452-461, src/streamCEOs.cpp:179-189).
+ *
+ * Objects are not thread-safe: one host thread at a time per handle.
+ */
+#ifndef CEOS_GB300_H
+#define CEOS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CEOS_ABI_VERSION 1
+
+#define CEOS_OK 0
+#define CEOS_ERR_ARG (-1)             /* invalid argument / shape */
+#define CEOS_ERR_NOT_BUILT (-2)       /* search or update before build */
+#define CEOS_ERR_PROBED_POINTS (-3)   /* n_probed_points > top_m (src/CEOs.cpp:452-456) */
+#define CEOS_ERR_PROBED_VECTORS (-4)  /* n_probed_vectors > n_proj*n_repeats (src/CEOs.cpp:457-461);
+                                         streamCEOs: > n_proj (src/streamCEOs.cpp:386-390) */
+#define CEOS_ERR_UPDATE_DEL (-5)      /* n_delPoints > current size (src/streamCEOs.cpp:179-183) */
+#define CEOS_ERR_UPDATE_TOPM (-6)     /* top_m > size after update (src/streamCEOs.cpp:185-189) */
+#define CEOS_ERR_CUDA (-7)            /* CUDA runtime error */
+#define CEOS_ERR_NO_DEVICE (-8)       /* no CUDA device visible */
+#define CEOS_ERR_UNSUPPORTED (-9)     /* size outside what the kernels support */
+#define CEOS_ERR_DEVICE_LIMIT (-10)   /* a bounded device-side loop gave up */
+
+/* Search algorithms for ceos_search_device. */
+#define CEOS_ALGO_DENSE 0   /* CEOs-Est:   build / search */
+#define CEOS_ALGO_COCEOS 1  /* coCEOs-Est: build_coCEOs_Est / search_coCEOs_Est */
+#define CEOS_ALGO_HASH 2    /* CEOs-Hash:  build_CEOs_Hash / search_CEOs_Hash */
+
+/* Numeric form of build and search. */
+#define CEOS_PRECISION_FP32 0       /* bit-exact FP32 projections, FP32 rerank */
+#define CEOS_PRECISION_SPLIT_BF16 1 /* BF16 rerank scan + FP32 rescore of the top 4k */
+
+typedef struct ceos_index ceos_index;
+typedef struct ceos_stream ceos_stream;
+
+/* ---- library ---------------------------------------------------------- */
+int ceos_abi_version(void);
+const char* ceos_last_error(void);
+/* Number of visible CUDA devices (0 when none); never fails. */
+int ceos_device_count(void);
+/* 0 = silent, 1 = the reference's build/search prints (src/CEOs.cpp:20-25,
+ * :90-97, :278-294). Default from env CEOS_GB300_LOG, else 1. */
+void ceos_set_log_level(int level);
+
+/* ---- CEOs (src/CEOs.h:18-114) ----------------------------------------- */
+/* CEOs(n_points, n_features): python/python_wrapper.cpp:14-21, src/CEOs.h:58-61 */
+int ceos_create(int n_points, int n_features, ceos_index** out);
+/* ~CEOs(): src/CEOs.h:113 */
+void ceos_destroy(ceos_index* h);
+/* setIndexParam(n_proj, n_repeats=1, top_m=10, n_threads=-1, random_seed=-1):
+ * python/python_wrapper.cpp:23-30 -> CEOs::set_CEOsParam, src/CEOs.h:63-81.
+ * Also resets n_probed_points = top_m as the reference does. */
+int ceos_set_index_param(ceos_index* h, int n_proj, int n_repeats, int top_m, int n_threads,
+                         int random_seed);
+int ceos_get_index_param(const ceos_index* h, int* n_proj, int* n_repeats, int* top_m,
+                         int* n_threads, int* random_seed, int* fht_dim);
+/* set_threads(n_threads): python/python_wrapper.cpp:36 -> src/CEOs.h:96-102 (kept for API
+ * compatibility; the GPU path does not use host threads). */
+int ceos_set_threads(ceos_index* h, int n_threads);
+/* clear(): python/python_wrapper.cpp:37 -> src/CEOs.h:83-89 (frees device memory). */
+int ceos_clear(ceos_index* h);
+/* n_probed_vectors / n_probed_points / n_cand attributes:
+ * python/python_wrapper.cpp:32-34 (defaults 10/10/10, src/CEOs.h:52-54). */
+int ceos_set_query_param(ceos_index* h, int n_probed_vectors, int n_probed_points, int n_cand);
+int ceos_get_query_param(const ceos_index* h, int* n_probed_vectors, int* n_probed_points,
+                         int* n_cand);
+/* centering attribute: python/python_wrapper.cpp:35 (src/CEOs.h:55). Stored only; see
+ * ceos_build_ceos_hash. */
+int ceos_set_centering(ceos_index* h, int centering);
+int ceos_get_centering(const ceos_index* h, int* centering);
+/* CEOS_PRECISION_* for the next search (no counterpart in the reference). */
+int ceos_set_precision(ceos_index* h, int precision);
+
+/* build(dataset): python/python_wrapper.cpp:39 -> CEOs::build_CEOs, src/CEOs.cpp:18-98.
+ * X: host, n_points x n_features float32 row-major. */
+int ceos_build(ceos_index* h, const float* X);
+/* search(queries, n_neighbors, verbose=False): python/python_wrapper.cpp:40-41 ->
+ * CEOs::search_CEOs, src/CEOs.cpp:107-297. Q host n_queries x n_features; ids/dists host
+ * n_queries x n_neighbors, best first, zero filled past the number of results. */
+int ceos_search(ceos_index* h, const float* Q, int n_queries, int n_neighbors, int verbose,
+                int32_t* ids, float* dists);
+/* build_coCEOs_Est: python/python_wrapper.cpp:43 -> src/CEOs.cpp:311-441 */
+int ceos_build_coceos_est(ceos_index* h, const float* X);
+/* search_coCEOs_Est: python/python_wrapper.cpp:44-45 -> src/CEOs.cpp:450-694 */
+int ceos_search_coceos_est(ceos_index* h, const float* Q, int n_queries, int n_neighbors,
+                           int verbose, int32_t* ids, float* dists);
+/* build_CEOs_Hash: python/python_wrapper.cpp:46 -> src/CEOs.cpp:708-840. The reference's
+ * centering branch (src/CEOs.cpp:721-728) subtracts an n-vector of row means and is not
+ * well defined; the flag is accepted and ignored. */
+int ceos_build_ceos_hash(ceos_index* h, const float* X);
+/* search_CEOs_Hash: python/python_wrapper.cpp:47-48 -> src/CEOs.cpp:850-1066 (n_cand unused,
+ * as in the reference). */
+int ceos_search_ceos_hash(ceos_index* h, const float* Q, int n_queries, int n_neighbors,
+                          int verbose, int32_t* ids, float* dists);
+/* Device-resident search (no reference counterpart: the queries and results already live in
+ * HBM). algo = CEOS_ALGO_*, which must match the built index. */
+int ceos_search_device(ceos_index* h, int algo, const float* d_Q, int n_queries,
+                       int n_neighbors, int32_t* d_ids, float* d_dists, void* cuda_stream);
+
+/* ---- introspection (no reference counterpart; used by parity tests) ---- */
+/* Buckets of a coCEOs-Est / CEOs-Hash index as [n_proj*n_repeats][2][top_m] ids and values
+ * (end 0 = closest, values v; end 1 = furthest, values -v): the reference's matrix_P
+ * (src/CEOs.cpp:417-428) / matrix_H (:819-828) in a column-end-major layout. */
+int ceos_get_buckets(const ceos_index* h, int32_t* ids, float* vals);
+/* Dense CEOs-Est projections as row-major n_points x (n_proj*n_repeats). */
+int ceos_get_projections(const ceos_index* h, float* P);
+/* The 3*n_repeats*fht_dim sign bits (1 = +1) in the reference's bit order. */
+int ceos_get_sign_bits(const ceos_index* h, uint8_t* bits);
+/* Per-phase device times (ms) of the last build/search, measured with CUDA events on the
+ * index's stream; returns the number of phases written. Phase names via
+ * ceos_timing_name. */
+int ceos_last_timings(const ceos_index* h, float* ms, int max_phases);
+const char* ceos_timing_name(const ceos_index* h, int phase);
+
+/* ---- streamCEOs (src/streamCEOs.h:12-107) ------------------------------ */
+/* streamCEOs(n_features): python/python_wrapper.cpp:52-53 */
+int ceos_stream_create(int n_features, ceos_stream** out);
+void ceos_stream_destroy(ceos_stream* h);
+/* setIndexParam(n_proj, n_repeats=1, top_points=1, n_threads=-1, random_seed=-1):
+ * python/python_wrapper.cpp:55-57 -> src/streamCEOs.h:53-70 (sets n_probed_vectors = top_m,
+ * as the reference does). */
+int ceos_stream_set_index_param(ceos_stream* h, int n_proj, int n_repeats, int top_points,
+                                int n_threads, int random_seed);
+int ceos_stream_set_threads(ceos_stream* h, int n_threads);
+int ceos_stream_clear(ceos_stream* h);
+int ceos_stream_set_query_param(ceos_stream* h, int n_probed_vectors, int n_probed_points,
+                                int n_cand);
+int ceos_stream_get_query_param(const ceos_stream* h, int* n_probed_vectors,
+                                int* n_probed_points, int* n_cand);
+/* build(dataset): python/python_wrapper.cpp:65 -> src/streamCEOs.cpp:9-161 */
+int ceos_stream_build(ceos_stream* h, const float* X, int n_points);
+/* update(new_dataset, n_delPoints=0): python/python_wrapper.cpp:66 ->
+ * src/streamCEOs.cpp:174-369 (append at the back, delete n_del from the front). */
+int ceos_stream_update(ceos_stream* h, const float* X_new, int n_new, int n_del);
+/* estimate_search: python/python_wrapper.cpp:67-68 -> src/streamCEOs.cpp:378-612 */
+int ceos_stream_estimate_search(ceos_stream* h, const float* Q, int n_queries, int n_neighbors,
+                                int verbose, int32_t* ids, float* dists);
+/* hash_search: python/python_wrapper.cpp:69-70 -> src/streamCEOs.cpp:621-877 */
+int ceos_stream_hash_search(ceos_stream* h, const float* Q, int n_queries, int n_neighbors,
+                            int verbose, int32_t* ids, float* dists);
+/* Current number of points (the reference's deque_X.size()). */
+int ceos_stream_size(const ceos_stream* h, int* n_points);
+int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CEOS_GB300_H */

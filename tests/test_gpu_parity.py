@@ -1,0 +1,270 @@
+"""GPU parity: the CUDA library (through its C ABI) against the CPU oracle.
+
+Bit-exact expectations (same tie rule on both sides):
+  * projections (sign flips + FWHT, src/CEOs.cpp:58-88) - every bit;
+  * bucket ids and values (src/CEOs.cpp:377-428);
+  * search ids and scores (both compute the score as a sequential FMA chain).
+Estimates are accumulated in the reference's probe pop order on both sides,
+so candidate sets match exactly too.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import gaussian_queries, gist_like, netflix_like, recall, sift_like
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32),
+                          np.asarray(b, np.float32).view(np.uint32))
+
+
+def build_pair(gpu, oracle, X, D, R, m, seed, kind="coceos"):
+    n, d = X.shape
+    g = gpu.CEOs(n, d)
+    o = oracle.CEOs(n, d)
+    for idx in (g, o):
+        idx.setIndexParam(D, R, m, 4, seed)
+        if kind == "coceos":
+            idx.build_coCEOs_Est(X)
+        elif kind == "hash":
+            idx.build_CEOs_Hash(X)
+        else:
+            idx.build(X)
+    return g, o
+
+
+@pytest.mark.parametrize("n,d,D,R", [
+    (200, 300, 1024, 2),   # config-0 shape: F = 1024
+    (300, 128, 256, 3),    # F = 256
+    (257, 150, 256, 2),    # row padding (150 -> 152)
+    (100, 5, 4, 2),        # F = 8
+    (64, 1, 2, 1),         # F = 2
+    (80, 33, 16, 2),       # n_proj < n_features: F = 64, keep 16
+    (45, 700, 512, 1),     # F = 1024 from d, D < F
+    (40, 2000, 512, 1),    # F = 2048
+    (33, 3000, 4096, 1),   # F = 4096
+    (90, 20, 32, 5),       # F = 32 (single phase)
+])
+def test_projection_bitexact(gpu, oracle, n, d, D, R):
+    X = netflix_like(n, d, seed=n + d)
+    X[3] = 0.0  # a zero row: signs of zero must match too
+    g = gpu.CEOs(n, d)
+    g.setIndexParam(D, R, 10, 1, 42)
+    g.build(X)
+    P = g.projections()
+    ref = oracle.project(X, D, R, 42)
+    assert bits_equal(P, ref)
+    assert np.array_equal(g.sign_bits(), oracle.sign_bits(3 * R * g.fhtDim, 42))
+
+
+@pytest.mark.parametrize("dist,n,d,D,R,m", [
+    ("netflix", 2000, 300, 1024, 2, 100),
+    ("sift", 3000, 128, 256, 4, 64),      # integer projections: exact ties
+    ("gist", 1500, 96, 128, 2, 150),
+    ("netflix", 500, 17, 16, 3, 500),     # top_m == n
+])
+def test_coceos_buckets_exact(gpu, oracle, dist, n, d, D, R, m):
+    gen = {"netflix": netflix_like, "sift": sift_like, "gist": gist_like}[dist]
+    X = gen(n, d, seed=11)
+    g, o = build_pair(gpu, oracle, X, D, R, m, 7)
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi)
+    assert bits_equal(gv, ov)
+
+
+@pytest.mark.parametrize("dist,n,d,D,R,m,s,c,k", [
+    ("netflix", 2000, 300, 1024, 2, 100, 20, 500, 10),
+    ("sift", 3000, 128, 256, 4, 64, 40, 300, 100),
+    ("gist", 1500, 96, 128, 2, 150, 12, 200, 1),
+])
+def test_coceos_search_exact(gpu, oracle, dist, n, d, D, R, m, s, c, k):
+    gen = {"netflix": netflix_like, "sift": sift_like, "gist": gist_like}[dist]
+    X = gen(n, d, seed=12)
+    Q = gen(64, d, seed=13) if dist != "netflix" else gaussian_queries(64, d, seed=13)
+    g, o = build_pair(gpu, oracle, X, D, R, m, 42)
+    for idx in (g, o):
+        idx.n_probed_vectors, idx.n_cand = s, c
+    gi, gd = g.search_coCEOs_Est(Q, k)
+    oi, od = o.search_coCEOs_Est(Q, k)
+    assert np.array_equal(gi, oi)
+    assert bits_equal(gd, od)
+    # n_probed_points below top_m
+    for idx in (g, o):
+        idx.n_probed_points = m // 3
+    gi, gd = g.search_coCEOs_Est(Q, k)
+    oi, od = o.search_coCEOs_Est(Q, k)
+    assert np.array_equal(gi, oi) and bits_equal(gd, od)
+
+
+def test_golden_fixture(gpu):
+    f = np.load(os.path.join(GOLD, "search_small.npz"))
+    D, R, m, s, c, k, seed = [int(v) for v in f["params"]]
+    X, Q = f["X"], f["Q"]
+    g = gpu.CEOs(*X.shape)
+    g.setIndexParam(D, R, m, 1, seed)
+    g.build_coCEOs_Est(X)
+    bi, bv = g.buckets()
+    assert np.array_equal(bi, f["bucket_ids"]) and bits_equal(bv, f["bucket_vals"])
+    g.n_probed_vectors, g.n_cand = s, c
+    ids, dists = g.search_coCEOs_Est(Q, k)
+    assert np.array_equal(ids, f["ids"]) and bits_equal(dists, f["dists"])
+
+
+def test_dense_search_exact(gpu, oracle):
+    n, d = 3000, 300
+    X = netflix_like(n, d, seed=21)
+    Q = gaussian_queries(40, d, seed=22)
+    g, o = build_pair(gpu, oracle, X, 512, 2, 10, 42, kind="dense")
+    for idx in (g, o):
+        idx.n_probed_vectors, idx.n_cand = 20, 300
+    gi, gd = g.search(Q, 10)
+    oi, od = o.search(Q, 10)
+    assert np.array_equal(gi, oi) and bits_equal(gd, od)
+
+
+def test_hash_search_exact(gpu, oracle):
+    n, d = 2500, 128
+    X = sift_like(n, d, seed=31)
+    Q = sift_like(40, d, seed=32)
+    g, o = build_pair(gpu, oracle, X, 256, 2, 50, 42, kind="hash")
+    gi, _ = g.buckets()
+    oi, _ = o.buckets()
+    assert np.array_equal(gi, oi)
+    for idx in (g, o):
+        idx.n_probed_vectors, idx.n_probed_points = 30, 20
+    ai, ad = g.search_CEOs_Hash(Q, 10)
+    bi, bd = o.search_CEOs_Hash(Q, 10)
+    assert np.array_equal(ai, bi) and bits_equal(ad, bd)
+
+
+def test_stream_fifo_exact(gpu, oracle):
+    d = 64
+    X = netflix_like(6000, d, seed=41)
+    Q = gaussian_queries(32, d, seed=42)
+    g, o = gpu.streamCEOs(d), oracle.streamCEOs(d)
+    for s in (g, o):
+        s.setIndexParam(128, 2, 40, 2, 42)
+        s.build(X[:2000])
+        s.n_probed_vectors, s.n_probed_points, s.n_cand = 20, 40, 200
+    steps = [(2000, 2500, 300), (2500, 4000, 1000), (4000, 4000, 700), (4000, 4100, 0),
+             (4100, 6000, 1900)]
+    for a, b, nd in steps:
+        for s in (g, o):
+            s.update(X[a:b], nd)
+        assert g.size == o.size
+        gi, gv = g.buckets()
+        oi, ov = o.buckets()
+        assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+        ai, ad = g.estimate_search(Q, 10)
+        bi, bd = o.estimate_search(Q, 10)
+        assert np.array_equal(ai, bi) and bits_equal(ad, bd)
+        ai, ad = g.hash_search(Q, 10)
+        bi, bd = o.hash_search(Q, 10)
+        assert np.array_equal(ai, bi) and bits_equal(ad, bd)
+
+
+def test_stream_stale_rows_quirk(gpu, oracle):
+    """Deleting most points with few new ones leaves stale bucket rows
+    (src/streamCEOs.cpp:331-352); both sides keep them identically."""
+    d = 16
+    X = netflix_like(400, d, seed=51)
+    g, o = gpu.streamCEOs(d), oracle.streamCEOs(d)
+    for s in (g, o):
+        s.setIndexParam(32, 1, 30, 1, 3)
+        s.build(X[:200])
+        s.update(X[200:215], 180)   # 35 points left, survivors + new may be < 30
+        s.update(X[215:230], 5)
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+
+
+def test_edge_cases(gpu, oracle):
+    n, d = 600, 24
+    X = netflix_like(n, d, seed=61)
+    X[100:140] = X[99]      # duplicated rows -> exact ties
+    X[200:210] = 0.0        # zero rows
+    Q = gaussian_queries(9, d, seed=62)
+    g, o = build_pair(gpu, oracle, X, 32, 2, 30, 5)
+    # fewer candidates than n_cand and k > candidates: zero fill
+    for s_, p_, c_, k_ in [(0, 30, 10, 5), (1, 3, 100, 8), (64, 30, 10000, 40), (5, 0, 10, 3)]:
+        for idx in (g, o):
+            idx.n_probed_vectors, idx.n_probed_points, idx.n_cand = s_, p_, c_
+        a = g.search_coCEOs_Est(Q, k_)
+        b = o.search_coCEOs_Est(Q, k_)
+        assert np.array_equal(a[0], b[0]) and bits_equal(a[1], b[1]), (s_, p_, c_, k_)
+    ids, dists = g.search_coCEOs_Est(Q[:0], 5)
+    assert ids.shape == (0, 5)
+    ids, dists = g.search_coCEOs_Est(Q, 0)
+    assert ids.shape == (9, 0)
+
+
+def test_param_errors_gpu(gpu):
+    n, d = 300, 16
+    g = gpu.CEOs(n, d)
+    g.setIndexParam(32, 2, 20, 1, 1)
+    g.build_coCEOs_Est(netflix_like(n, d))
+    g.n_probed_points = 21
+    with pytest.raises(ValueError, match="probed points"):
+        g.search_coCEOs_Est(gaussian_queries(2, d), 3)
+    g.n_probed_points = 20
+    g.n_probed_vectors = 65
+    with pytest.raises(ValueError, match="probed vectors"):
+        g.search_coCEOs_Est(gaussian_queries(2, d), 3)
+    with pytest.raises(ValueError):
+        g.setIndexParam(32, 2, 301, 1, 1)
+        g.build_coCEOs_Est(netflix_like(n, d))
+    s = gpu.streamCEOs(d)
+    s.setIndexParam(32, 2, 20, 1, 1)
+    s.build(netflix_like(100, d))
+    with pytest.raises(ValueError, match="removed points"):
+        s.update(netflix_like(1, d), 200)
+    with pytest.raises(ValueError, match="not enough"):
+        s.update(netflix_like(1, d), 90)
+    s.n_probed_points = 10
+    s.n_probed_vectors = 33  # stream limit is n_proj (src/streamCEOs.cpp:386-390)
+    with pytest.raises(ValueError, match="probed vectors"):
+        s.estimate_search(gaussian_queries(2, d), 3)
+
+
+def test_sampled_thresholds_large_n(gpu, oracle):
+    """n > 65536 takes the strided-sample threshold path; buckets stay exact."""
+    n, d = 150000, 32
+    X = sift_like(n, d, seed=71)
+    g, o = build_pair(gpu, oracle, X, 64, 2, 60, 9)
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+
+
+def test_exact_fallback_on_massive_ties(gpu, oracle):
+    """70% identical rows overflow the candidate lists of the columns where
+    they rank at the top; those column ends go through the exact fallback."""
+    n, d = 100000, 16
+    rng = np.random.default_rng(81)
+    X = netflix_like(n, d, seed=81)
+    dup = rng.random(n) < 0.7
+    X[dup] = X[0] * 3.0
+    g, o = build_pair(gpu, oracle, X, 32, 1, 50, 13)
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+
+
+def test_recall_vs_fp64(gpu, oracle):
+    n, d = 20000, 300
+    X = netflix_like(n, d, seed=91)
+    Q = gaussian_queries(100, d, seed=92)
+    gt, _ = oracle.bruteforce(X, Q, 10)
+    g = gpu.CEOs(n, d)
+    g.setIndexParam(1024, 2, 100, 1, 42)
+    g.build_coCEOs_Est(X)
+    g.n_probed_vectors, g.n_cand = 20, 500
+    ids, dists = g.search_coCEOs_Est(Q, 10)
+    assert recall(ids, gt) > 0.85
