@@ -1,0 +1,351 @@
+"""Benchmark of the CEOs index path on GB300.
+
+Workload (default): plain FP32 coCEOs-Est build + search at scale,
+X = 1,000,000 x 128 float32 (70% round(Gamma(0.8, 30)) clipped to [0, 255],
+30% exact zeros), 10,000 queries from the same distribution, n_proj=256,
+n_repeats=8, top_m=500, n_probed_vectors=40, n_cand=2000, k=10 (seeded
+synthetic data with the shapes and value distribution of the SIFT benchmark).
+
+A step is one search of the 10,000-query batch. ``value`` is queries/s with
+the queries already resident in HBM, timed with the library's CUDA events on
+its launch stream; ``e2e`` is the same metric through the host-buffer C-ABI
+call (host->device copy of the queries and device->host copy of ids and
+scores inside the timed region). The L2 is flushed before every timed step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path is replicated, not sharded) and rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import ctypes.util
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(n=1_000_000, d=128, nq=10_000, D=256, R=8, m=500, s=40, c=2000, k=10, seed=42)
+WORKLOAD = "coCEOs-Est FP32 build+search, SIFT-shaped 1Mx128, 10k queries"
+
+
+def sift_like(n, d, seed):
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, d), np.float32)
+    step = 200_000
+    for i in range(0, n, step):
+        j = min(n, i + step)
+        v = np.clip(np.round(rng.gamma(0.8, 30.0, (j - i, d))), 0, 255).astype(np.float32)
+        v[rng.random((j - i, d)) < 0.3] = 0.0
+        out[i:j] = v
+    return out
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        j = json.load(open(p))
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Cudart:
+    """Minimal cudart access for device buffers (the product itself does not
+    need it: this is only how the benchmark places its queries in HBM)."""
+
+    def __init__(self):
+        cands = ["/usr/local/cuda/lib64/libcudart.so", ctypes.util.find_library("cudart")]
+        for c in cands:
+            if c and (os.path.exists(c) or not c.startswith("/")):
+                try:
+                    self.L = C.CDLL(c)
+                    break
+                except OSError:
+                    continue
+        else:
+            raise RuntimeError("libcudart not found")
+        self.L.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        self.L.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        self.L.cudaFree.argtypes = [C.c_void_p]
+
+    def malloc(self, nbytes):
+        p = C.c_void_p()
+        if self.L.cudaMalloc(C.byref(p), nbytes) != 0:
+            raise RuntimeError("cudaMalloc failed")
+        return p.value
+
+    def h2d(self, dst, arr):
+        if self.L.cudaMemcpy(C.c_void_p(dst), arr.ctypes.data, arr.nbytes, 1) != 0:
+            raise RuntimeError("cudaMemcpy H2D failed")
+
+    def d2h(self, arr, src):
+        if self.L.cudaMemcpy(arr.ctypes.data, C.c_void_p(src), arr.nbytes, 2) != 0:
+            raise RuntimeError("cudaMemcpy D2H failed")
+
+    def free(self, p):
+        self.L.cudaFree(C.c_void_p(p))
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.fh.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        # one replica per GPU: pin this rank to its GPU before the library
+        # creates a CUDA context
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", "0")
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return ws, rank, dist
+    return 1, 0, None
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_baseline_run(X, Q, n_queries, threads):
+    """Oracle restatement of the reference's OpenMP path on the host cores:
+    build the index, then search a bounded sample of queries."""
+    from oracle import oracle as O
+
+    idx = O.CEOs(*X.shape)
+    idx.setIndexParam(CFG["D"], CFG["R"], CFG["m"], threads, CFG["seed"])
+    t0 = time.perf_counter()
+    idx.build_coCEOs_Est(X)
+    build_s = time.perf_counter() - t0
+    idx.n_probed_vectors, idx.n_cand = CFG["s"], CFG["c"]
+    t0 = time.perf_counter()
+    idx.search_coCEOs_Est(Q[:n_queries], CFG["k"])
+    dt = time.perf_counter() - t0
+    return n_queries / dt, build_s, idx
+
+
+def run_reference(args, X, Q):
+    ws, rank, dist = dist_setup()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    sample = args.ref_queries
+    qps, build_s, idx = cpu_baseline_run(X, Q, 16, threads)
+    for _ in range(args.warmup):
+        idx.search_coCEOs_Est(Q[:sample], CFG["k"])
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        off = (i * sample) % (len(Q) - sample)
+        idx.search_coCEOs_Est(Q[off:off + sample], CFG["k"])
+    dt = time.perf_counter() - t0
+    value = args.steps * sample / dt
+    line = {"impl": "reference", "metric": "queries/s at recall@10 (coCEOs-Est search)",
+            "value": value, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " (CPU oracle port, all host threads)", **CFG,
+                       "queries_per_step": sample},
+            "build_s": build_s,
+            "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{sample} queries per step on the full 1Mx128 index"},
+            "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--ref-queries", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--recall-queries", type=int, default=200)
+    args = ap.parse_args()
+    os.environ.setdefault("CEOS_GB300_LOG", "0")
+
+    X = sift_like(CFG["n"], CFG["d"], 7)
+    Q = sift_like(CFG["nq"], CFG["d"], 8)
+    if args.impl == "reference":
+        return run_reference(args, X, Q)
+
+    ws, rank, dist = dist_setup()
+    import ceos_gb300.CEOs as CEOs
+    from ceos_gb300 import _capi
+
+    L = _capi.lib()
+    L.ceos_set_log_level(0)
+    if L.ceos_device_count() < 1:
+        raise SystemExit("bench.py needs a CUDA device")
+    rt = Cudart()
+
+    idx = CEOs.CEOs(CFG["n"], CFG["d"])
+    idx.setIndexParam(CFG["D"], CFG["R"], CFG["m"], -1, CFG["seed"])
+    t0 = time.perf_counter()
+    idx.build_coCEOs_Est(X)
+    build_s = time.perf_counter() - t0
+    build_phases = idx.last_timings()
+    idx.n_probed_vectors, idx.n_cand = CFG["s"], CFG["c"]
+    nq, k, d = CFG["nq"], CFG["k"], CFG["d"]
+
+    dQ = rt.malloc(Q.nbytes)
+    dI = rt.malloc(nq * k * 4)
+    dD = rt.malloc(nq * k * 4)
+    rt.h2d(dQ, Q)
+    flush = 512 << 20
+
+    def dev_step():
+        idx.search_device(_capi.ALGO_COCEOS, dQ, nq, k, dI, dD)
+        return idx.last_timings()
+
+    for _ in range(args.warmup):
+        dev_step()
+    clocks = ClockSampler(0)
+    barrier(dist)
+    clocks.start()
+    step_ms, kern_ms = [], []
+    for _ in range(args.steps):
+        _capi.check(L.ceos_flush_l2(flush))
+        t = dev_step()
+        step_ms.append(sum(t.values()))
+        kern_ms.append(t["estimate+rerank"])
+    barrier(dist)
+    clk = clocks.stop()
+    dev_total_s = max_over_ranks(dist, sum(step_ms) / 1e3)
+    value = ws * args.steps * nq / dev_total_s
+
+    # end to end through the host-buffer C ABI
+    e2e_t = []
+    for _ in range(max(1, args.warmup)):
+        idx.search_coCEOs_Est(Q, k)
+    for _ in range(args.steps):
+        _capi.check(L.ceos_flush_l2(flush))
+        t0 = time.perf_counter()
+        ids, dists = idx.search_coCEOs_Est(Q, k)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_total = max_over_ranks(dist, sum(e2e_t))
+    e2e_value = ws * args.steps * nq / e2e_total
+
+    # device results equal host-call results
+    hi = np.zeros((nq, k), np.int32)
+    rt.d2h(hi, dI)
+    assert np.array_equal(hi, ids), "device-resident and host-call results differ"
+
+    # roofline of the dominant kernel (query estimate + rerank)
+    s, p, c, m, C_ = CFG["s"], CFG["m"], CFG["c"], CFG["m"], CFG["D"] * CFG["R"]
+    bytes_per_query = s * p * 8 + c * d * 4 + C_ * 4 + d * 4 + k * 8
+    kern_s = float(np.mean(kern_ms)) / 1e3
+    achieved = bytes_per_query * nq / kern_s / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("query_estimate_rerank_bytes_per_launch")
+
+    # recall@10 against float64 brute force on a sample of queries
+    from oracle import oracle as O
+
+    rq = args.recall_queries
+    gt, _ = O.bruteforce(X, Q[:rq], 10, 0)
+    rec = float(np.mean([len(np.intersect1d(a, b)) / 10 for a, b in zip(ids[:rq], gt)]))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        qps, cpu_build_s, _ = cpu_baseline_run(X, Q, 64, threads)
+        cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": "64 queries searched on the full 1Mx128 index built by the oracle",
+               "build_s": cpu_build_s}
+
+    if rank == 0:
+        line = {
+            "metric": "queries/s at recall@10 (coCEOs-Est search)",
+            "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_total_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, **CFG, "l2": "flushed (512 MiB write) before every step",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "recall@10": rec, "recall_queries": rq,
+            "build_s": build_s, "build_phases_ms": build_phases,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_query_buckets<estimate>",
+                         "bytes_per_query": bytes_per_query, "kernel_ms": kern_s * 1e3},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": Q.nbytes,
+                    "d2h_bytes_per_step": nq * k * 8},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    rt.free(dQ)
+    rt.free(dI)
+    rt.free(dD)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -42,6 +42,7 @@ SIGNATURES = {
     "ceos_last_error": (C.c_char_p, []),
     "ceos_device_count": (C.c_int, []),
     "ceos_set_log_level": (None, [C.c_int]),
+    "ceos_flush_l2": (C.c_int, [C.c_long]),
     "ceos_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(VP)]),
     "ceos_destroy": (None, [VP]),
     "ceos_set_index_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),

@@ -568,6 +568,16 @@ int ceos_device_count(void) {
 }
 void ceos_set_log_level(int level) { g_log = level < 0 ? 0 : level; }
 
+int ceos_flush_l2(long bytes) {
+  static DevBuf* flush = nullptr;
+  if (bytes <= 0) return fail(CEOS_ERR_ARG, "bytes must be > 0");
+  if (!flush) flush = new DevBuf();
+  CUDA_TRY(flush->ensure((size_t)bytes));
+  CUDA_TRY(cudaMemsetAsync(flush->p, 0x5a, (size_t)bytes, 0));
+  CUDA_TRY(cudaDeviceSynchronize());
+  return CEOS_OK;
+}
+
 // ---------------------------------------------------------------------------
 int ceos_create(int n_points, int n_features, ceos_index** out) {
   if (!out) return fail(CEOS_ERR_ARG, "null output handle");

@@ -23,6 +23,12 @@ namespace ceos {
 
 // Work split: each warp processes V rows (V vectors) at a time, all R
 // repeats, grid-striding over row groups.
+// Warps per CTA: 8, or 4 when two 4096-float vectors per warp would not fit.
+template <int L>
+constexpr int proj_warps() {
+  return L >= 12 ? 4 : 8;
+}
+
 template <int L, int MODE>
 __global__ void __launch_bounds__(256) k_project(ProjArgs a) {
   using Cfg = FwhtCfg<L>;
@@ -108,7 +114,7 @@ template <int L>
 static size_t proj_smem(int R) {
   using Cfg = FwhtCfg<L>;
   size_t sw = ((size_t)R * 3 * Cfg::words * 4 + 15) & ~(size_t)15;
-  return sw + (size_t)8 * 2 * Cfg::V * Cfg::Vstride * sizeof(float);
+  return sw + (size_t)proj_warps<L>() * 2 * Cfg::V * Cfg::Vstride * sizeof(float);
 }
 
 template <int L, int MODE>
@@ -118,16 +124,17 @@ cudaError_t launch_L(const ProjArgs& a, int num_sms, cudaStream_t st) {
                                        (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project<L, MODE>, 256, smem);
+  constexpr int threads = 32 * proj_warps<L>();
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project<L, MODE>, threads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   using Cfg = FwhtCfg<L>;
   const long groups = (a.n_rows + Cfg::V - 1) / Cfg::V;
-  long blocks = (groups + 7) / 8;
+  long blocks = (groups + proj_warps<L>() - 1) / proj_warps<L>();
   const long max_blocks = (long)num_sms * per_sm;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;
-  k_project<L, MODE><<<(unsigned)blocks, 256, smem, st>>>(a);
+  k_project<L, MODE><<<(unsigned)blocks, threads, smem, st>>>(a);
   return cudaGetLastError();
 }
 

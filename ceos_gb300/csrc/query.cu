@@ -61,13 +61,14 @@ CEOS_DEV float dot_seq(const float* __restrict__ q, const float* __restrict__ x,
 CEOS_DEV int slot_id(uint64_t w) { return (int)(uint32_t)(w & 0xffffffffu); }
 CEOS_DEV float slot_val(uint64_t w) { return __uint_as_float((uint32_t)(w >> 32)); }
 
-// Find or insert `id`; returns the slot index. The table never fills up
-// (capacity > number of insertions).
+// Find or insert `id`; returns the slot index. The capacity exceeds the
+// number of insertions, so a free slot always exists; the probe sequence is
+// still bounded by the capacity and returns -1 if it ever ran out.
 CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
   const uint32_t h = (uint32_t)id * 0x9E3779B1u;
   int s = (int)(((uint64_t)h * (uint32_t)cap) >> 32);
   int* keys = reinterpret_cast<int*>(t);
-  while (true) {
+  for (int probe = 0; probe < cap; ++probe) {
     const int cur = *reinterpret_cast<volatile int*>(&keys[2 * s]);
     if (cur == id) return s;
     if (cur == -1) {
@@ -76,6 +77,7 @@ CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
     }
     s = (s + 1 == cap) ? 0 : s + 1;
   }
+  return -1;
 }
 
 struct QLayout {
@@ -153,7 +155,11 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
       const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m;
       for (int e = threadIdx.x; e < a.p; e += blockDim.x) {
         const int id = __ldg(a.bids + base + e);
+        // streamCEOs can keep stale bucket rows whose id is no longer a live
+        // point; they are skipped (the reference reads out of range there).
+        if ((unsigned)id >= (unsigned long)a.n_points) continue;
         const int sl = table_slot(table, cap, id);
+        if (sl < 0) continue;
         if (MODE == Q_ESTIMATE) {
           const float v = __ldg(a.bvals + base + e);
           atomicAdd(reinterpret_cast<float*>(&table[sl]) + 1, v);

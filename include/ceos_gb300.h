@@ -64,6 +64,11 @@ int ceos_device_count(void);
  * :90-97, :278-294). Default from env CEOS_GB300_LOG, else 1. */
 void ceos_set_log_level(int level);
 
+/* Benchmark hygiene (no reference counterpart): overwrite `bytes` of a device
+ * buffer owned by the library (allocated on first use) so that the next timed
+ * call starts with a cold L2; synchronizes the device. */
+int ceos_flush_l2(long bytes);
+
 /* ---- CEOs (src/CEOs.h:18-114) ----------------------------------------- */
 /* CEOs(n_points, n_features): python/python_wrapper.cpp:14-21, src/CEOs.h:58-61 */
 int ceos_create(int n_points, int n_features, ceos_index** out);

@@ -38,6 +38,9 @@
 //    heap (src/CEOs.cpp:634-647 is undefined behaviour there).
 //  * Ids are int32 (the reference stores them as float inside matrix_P,
 //    exact only below 2^24 points).
+//  * streamCEOs searches skip bucket entries whose id is not a live point
+//    (stale rows left by update can hold such ids; the reference indexes
+//    deque_X out of range there).
 //
 // Pins: the FWHT is checked bit for bit against the reference's own FFHT
 // sources compiled by oracle/Makefile (target `ref`), and the sign generator
@@ -608,6 +611,10 @@ struct OracleStream {
           size_t o = (size_t)c * 2 * m + (tag < 0 ? m : 0);
           for (int j = 0; j < p; ++j) {
             int id = B_ids[o + j];
+            // A stale row (see update) can hold an id past the current size;
+            // the reference then reads deque_X out of range (undefined
+            // behaviour). Such entries are skipped.
+            if (id < 0 || id >= n_points) continue;
             float v = B_vals[o + j];
             auto it = est.find(id);
             if (it == est.end()) est[id] = v;
@@ -648,7 +655,10 @@ struct OracleStream {
         for (int tag : probes) {
           int c = tag < 0 ? -tag - 1 : tag - 1;
           size_t o = (size_t)c * 2 * m + (tag < 0 ? m : 0);
-          for (int j = 0; j < p; ++j) seen[B_ids[o + j]] = 1;
+          for (int j = 0; j < p; ++j) {
+            const int id = B_ids[o + j];
+            if (id >= 0 && id < n_points) seen[id] = 1;  // stale ids skipped, as above
+          }
         }
         MinQue topk;
         for (int i = 0; i < n_points; ++i)
