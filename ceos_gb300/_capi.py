@@ -61,6 +61,7 @@ SIGNATURES = {
     "ceos_build_ceos_hash": (C.c_int, [VP, F32P]),
     "ceos_search_ceos_hash": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
     "ceos_search_device": (C.c_int, [VP, C.c_int, VP, C.c_int, C.c_int, VP, VP, VP]),
+    "ceos_search_coceos_est_device_noalloc": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, VP]),
     "ceos_get_buckets": (C.c_int, [VP, I32P, F32P]),
     "ceos_get_projections": (C.c_int, [VP, F32P]),
     "ceos_get_sign_bits": (C.c_int, [VP, U8P]),

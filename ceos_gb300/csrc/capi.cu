@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <string>
 #include <vector>
@@ -1062,3 +1063,119 @@ int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free search.
+//
+// Some callers cannot let this library call cudaMalloc: a host process that
+// owns every byte of device memory through its own arena (a database or
+// search-engine plugin host), or a latency-critical serving loop in which an
+// allocation could stall the device or fail in the middle of a request. For
+// them, ceos_search_coceos_est_device_noalloc takes its scratch (the padded
+// queries, their projections and, when a query's hash table does not fit in
+// shared memory, the per-CTA tables) from the fixed array below instead of
+// allocating. The array is a file-scope __device__ object, so every GPU that
+// loads this library holds it until the process exits.
+constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;  // 64 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[128] = {};
+
+// Device address of g_noalloc_scratch on `dev` (which must be current). In
+// host code the symbol itself is only a host-side stand-in, so the address is
+// looked up once per device with cudaGetSymbolAddress and cached.
+int noalloc_scratch(int dev, void** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (dev < 0 || dev >= 128) return fail(CEOS_ERR_ARG, "device ordinal %d out of range", dev);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(CEOS_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CEOS_OK;
+}
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
+extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float* d_Q, int nq,
+                                                     int k, int32_t* d_ids, float* d_dists,
+                                                     void* cuda_stream) {
+  if (!h) return fail(CEOS_ERR_ARG, "null handle");
+  Core& c = h->core;
+  ST_TRY(check_query(c, B_COCEOS, 1, nq, k, c.C()));
+  if (nq == 0 || k == 0) return CEOS_OK;
+  if (!d_Q || !d_ids || !d_dists) return fail(CEOS_ERR_ARG, "null buffer");
+  CUDA_TRY(cudaSetDevice(c.device));
+  cudaStream_t st = cuda_stream ? reinterpret_cast<cudaStream_t>(cuda_stream) : c.stream;
+  // Scratch layout: padded queries | query projections | per-CTA hash tables.
+  QueryArgs q;
+  q.nq = nq;
+  q.d = c.n_features;
+  q.ldx = c.ldx;
+  q.C = c.C();
+  q.s = c.s;
+  q.p = c.p;
+  q.m = c.top_m;
+  q.c = c.c;
+  q.k = k;
+  q.X = c.dX.as<float>();
+  q.head = c.head;
+  q.cap_rows = c.cap_rows;
+  q.n_points = c.n_rows;
+  q.bids = c.dBids.as<int>();
+  q.bvals = c.dBvals.as<float>();
+  q.out_ids = d_ids;
+  q.out_d = d_dists;
+  const long pairs = (long)std::max(c.s, 0) * std::max(c.p, 0);
+  long tc = std::max(64L, pairs + pairs / 4 + 1);
+  tc = (tc + 31) & ~31L;
+  if (tc > INT_MAX / 2) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
+  q.table_cap = (int)tc;
+  q.table_in_smem = 1;
+  size_t smem = query_buckets_smem(q, Q_ESTIMATE);
+  int per_sm;
+  if (smem > c.smem_optin) {
+    q.table_in_smem = 0;
+    smem = query_buckets_smem(q, Q_ESTIMATE);
+    if (smem > c.smem_optin)
+      return fail(CEOS_ERR_UNSUPPORTED, "query working set exceeds shared memory");
+  }
+  per_sm = c.query_blocks_per_sm(Q_ESTIMATE, smem);
+  const int grid = (int)std::max<long>(1, std::min<long>(nq, (long)c.sms * std::max(per_sm, 1)));
+  const size_t qbytes = al256((size_t)nq * c.ldx * 4);
+  const size_t pbytes = al256((size_t)nq * c.C() * 4);
+  const size_t tbytes = q.table_in_smem ? 0 : (size_t)grid * tc * 8;
+  const size_t need = qbytes + pbytes + tbytes;
+  if (need > kNoAllocScratchBytes)
+    return fail(CEOS_ERR_UNSUPPORTED,
+                "this batch needs %zu bytes of scratch; the allocation-free search is limited to %zu "
+                "bytes (n_queries * (n_features + n_proj * n_repeats) * 4 plus hash tables): split "
+                "the batch",
+                need, kNoAllocScratchBytes);
+  void* base = nullptr;
+  ST_TRY(noalloc_scratch(c.device, &base));
+  unsigned char* sc = static_cast<unsigned char*>(base);
+  float* qpad = reinterpret_cast<float*>(sc);
+  float* qproj = reinterpret_cast<float*>(sc + qbytes);
+  q.gtable = q.table_in_smem ? nullptr : reinterpret_cast<uint64_t*>(sc + qbytes + pbytes);
+  q.Q = qpad;
+  q.qproj = qproj;
+  // Every buffer above is fully written before it is read (the hash tables
+  // are reset per query inside the kernel), so no clearing is needed.
+  CUDA_TRY(launch_pad_rows(d_Q, nq, c.n_features, qpad, c.ldx, st));
+  ProjArgs a = c.proj_base();
+  a.X = qpad;
+  a.head = 0;
+  a.cap_rows = LONG_MAX;
+  a.n_rows = nq;
+  a.out = qproj;
+  CUDA_TRY(launch_project(a, PROJ_ROWS, c.L, c.sms, st));
+  CUDA_TRY(launch_query_buckets(q, Q_ESTIMATE, grid, smem, st));
+  return CEOS_OK;
+}

@@ -124,6 +124,26 @@ int ceos_search_ceos_hash(ceos_index* h, const float* Q, int n_queries, int n_ne
 int ceos_search_device(ceos_index* h, int algo, const float* d_Q, int n_queries,
                        int n_neighbors, int32_t* d_ids, float* d_dists, void* cuda_stream);
 
+/* No counterpart in the reference. coCEOs-Est search over device-resident queries that
+ * allocates no device memory, for callers that cannot let the library call cudaMalloc: a
+ * host process that owns all device memory through its own arena (a database or search
+ * engine embedding the index as a plugin), or a latency-critical serving loop where an
+ * allocation could stall the device or fail mid-request. Same arguments and results as
+ * ceos_search_device(h, CEOS_ALGO_COCEOS, ...), but asynchronous: the results are valid once
+ * `cuda_stream` (NULL = the index's stream) has been synchronized.
+ * Scratch (padded queries, their projections, and per-CTA hash tables when a table does not
+ * fit in shared memory) comes from one fixed 64 MiB device array that every GPU loading the
+ * library holds until exit. A batch needing more than that is rejected with
+ * CEOS_ERR_UNSUPPORTED (roughly n_queries * (n_features + n_proj * n_repeats) * 4 bytes
+ * plus the tables): split it. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream capture. All calls
+ * share the array and it keeps the last call's contents, so calls whose GPU work overlaps
+ * (on different streams, or from different indexes on the same device) race: serialize
+ * them. */
+int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float* d_Q, int n_queries,
+                                          int n_neighbors, int32_t* d_ids, float* d_dists,
+                                          void* cuda_stream);
+
 /* ---- introspection (no reference counterpart; used by parity tests) ---- */
 /* Buckets of a coCEOs-Est / CEOs-Hash index as [n_proj*n_repeats][2][top_m] ids and values
  * (end 0 = closest, values v; end 1 = furthest, values -v): the reference's matrix_P
