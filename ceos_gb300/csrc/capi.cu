@@ -100,6 +100,23 @@ int np2(int x) {
   return p;
 }
 
+// Hash-table capacity for a query probing s columns of p entries: the
+// smallest prime >= max(64, 1.2 * s * p) (prime for double hashing), or -1
+// when it would not fit an int.
+long table_capacity(int s, int p) {
+  const long pairs = (long)std::max(s, 0) * std::max(p, 0);
+  long c = std::max(64L, pairs + pairs / 5 + 1);
+  if (c > INT_MAX / 4) return -1;
+  auto is_prime = [](long x) {
+    if (x < 2) return false;
+    for (long d = 2; d * d <= x; ++d)
+      if (x % d == 0) return false;
+    return true;
+  };
+  while (!is_prime(c)) ++c;
+  return c;
+}
+
 int ilog2(int F) {
   int l = 0;
   while ((1 << l) < F) ++l;
@@ -454,23 +471,21 @@ struct Core {
     }
     q.out_ids = out_ids;
     q.out_d = out_d;
-    const long pairs = (long)std::max(s, 0) * std::max(p, 0);
-    long tc = std::max(64L, pairs + pairs / 4 + 1);
-    tc = (tc + 31) & ~31L;
-    if (tc > INT_MAX / 2) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
+    const long tc = table_capacity(s, p);
+    if (tc < 0) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
     q.table_cap = (int)tc;
     q.table_in_smem = 1;
     size_t smem = query_buckets_smem(q, mode);
     int grid;
     if (smem <= smem_optin) {
-      int per_sm = query_blocks_per_sm(mode, smem);
+      int per_sm = query_blocks_per_sm(mode, smem, true);
       grid = (int)std::min<long>(nq, (long)sms * std::max(per_sm, 1));
     } else {
       q.table_in_smem = 0;
       smem = query_buckets_smem(q, mode);
       if (smem > smem_optin)
         return fail(CEOS_ERR_UNSUPPORTED, "query working set (n_cand=%d, n_neighbors=%d) exceeds shared memory", c, k);
-      int per_sm = query_blocks_per_sm(mode, smem);
+      int per_sm = query_blocks_per_sm(mode, smem, false);
       grid = (int)std::min<long>(nq, (long)sms * std::max(per_sm, 1));
       CUDA_TRY(wTable.ensure((size_t)grid * tc * 8));
       q.gtable = wTable.as<uint64_t>();
@@ -527,10 +542,12 @@ struct Core {
     return CEOS_OK;
   }
 
-  int query_blocks_per_sm(int mode, size_t smem);
+  int query_blocks_per_sm(int mode, size_t smem, bool table_in_smem);
 };
 
-int Core::query_blocks_per_sm(int mode, size_t smem) { return query_buckets_blocks_per_sm(mode, smem); }
+int Core::query_blocks_per_sm(int mode, size_t smem, bool table_in_smem) {
+  return query_buckets_blocks_per_sm(mode, smem, table_in_smem);
+}
 
 void print_timings(const char* what, const Timer& t) {
   if (log_level() < 1) return;
@@ -1132,10 +1149,8 @@ extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float*
   q.bvals = c.dBvals.as<float>();
   q.out_ids = d_ids;
   q.out_d = d_dists;
-  const long pairs = (long)std::max(c.s, 0) * std::max(c.p, 0);
-  long tc = std::max(64L, pairs + pairs / 4 + 1);
-  tc = (tc + 31) & ~31L;
-  if (tc > INT_MAX / 2) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
+  const long tc = table_capacity(c.s, c.p);
+  if (tc < 0) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
   q.table_cap = (int)tc;
   q.table_in_smem = 1;
   size_t smem = query_buckets_smem(q, Q_ESTIMATE);
@@ -1146,7 +1161,7 @@ extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float*
     if (smem > c.smem_optin)
       return fail(CEOS_ERR_UNSUPPORTED, "query working set exceeds shared memory");
   }
-  per_sm = c.query_blocks_per_sm(Q_ESTIMATE, smem);
+  per_sm = c.query_blocks_per_sm(Q_ESTIMATE, smem, q.table_in_smem != 0);
   const int grid = (int)std::max<long>(1, std::min<long>(nq, (long)c.sms * std::max(per_sm, 1)));
   const size_t qbytes = al256((size_t)nq * c.ldx * 4);
   const size_t pbytes = al256((size_t)nq * c.C() * 4);

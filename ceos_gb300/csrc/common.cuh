@@ -167,6 +167,228 @@ __device__ int block_topk_sorted(GetKey get, long N, int K, uint64_t* out, int c
   return cnt;
 }
 
+
+// ---------------------------------------------------------------------------
+// Block-level top-K by value histogram.
+//
+// Exact top-K (under the packed (value, id) order) of N items delivered by
+// `get(i, v, id) -> bool`. Three passes over the items instead of up to eight
+// radix passes:
+//   1. min / max / count of the values;
+//   2. a 2048-bin histogram on a LINEAR scale over [min, max], which spreads
+//      clustered values over many counters (a radix digit of the float key
+//      puts most of them on one shared-memory counter);
+//   3. compaction: items in bins above the threshold bin go straight to `out`,
+//      items of the threshold bin to `maybe`, which is then sorted by packed
+//      key to take the missing ones.
+// The bin index is a weakly increasing function of the value, so every item
+// of a higher bin ranks above every item of a lower bin, and ties in value
+// land in the same bin where the packed key orders them. Degenerate value
+// ranges, non-finite values and an oversized threshold bin fall back to the
+// radix select. `out` (at least K slots) receives min(K, valid) keys,
+// unsorted; with unique keys they are exactly the top-K.
+//
+// Shared memory: hist = kHistBins u32, maybe = maybe_cap u64 (power of two),
+// scratch = 16 u32. All threads of the block must call it; blockDim.x must be
+// a multiple of 32.
+constexpr int kHistBins = 2048;
+
+CEOS_DEV uint32_t warp_reserve(bool want, uint32_t* counter) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  uint32_t base = 0;
+  const int lane = threadIdx.x & 31;
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return base + __popc(m & ((1u << lane) - 1u));
+}
+
+template <typename GetItem>
+__device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32_t* hist,
+                               uint64_t* maybe, int maybe_cap, uint32_t* scratch) {
+  const int lane = threadIdx.x & 31;
+  // ---- pass 1: min / max keys and count ----
+  if (threadIdx.x == 0) {
+    scratch[0] = 0xffffffffu;  // min key
+    scratch[1] = 0u;           // max key
+    scratch[2] = 0u;           // valid count
+    scratch[3] = 0u;           // out count
+    scratch[4] = 0u;           // maybe count
+  }
+  __syncthreads();
+  {
+    uint32_t lo = 0xffffffffu, hi = 0u, cnt = 0u;
+    for (long i = threadIdx.x; i < N; i += blockDim.x) {
+      float v;
+      int id;
+      if (get(i, v, id)) {
+        const uint32_t k = fkey(v);
+        lo = min(lo, k);
+        hi = max(hi, k);
+        ++cnt;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0) {
+      atomicMin(&scratch[0], lo);
+      atomicMax(&scratch[1], hi);
+      atomicAdd(&scratch[2], cnt);
+    }
+  }
+  __syncthreads();
+  const uint32_t nvalid = scratch[2];
+  const float vmin = fkey_inv(scratch[0]), vmax = fkey_inv(scratch[1]);
+  if (K <= 0 || nvalid == 0) return 0;
+  if (nvalid <= (uint32_t)K) {
+    for (long base = 0; base < N; base += blockDim.x) {
+      const long i = base + threadIdx.x;
+      float v = 0.f;
+      int id = 0;
+      const bool ok = i < N && get(i, v, id);
+      const uint32_t pos = warp_reserve(ok, &scratch[3]);
+      if (ok) out[pos] = pack_key(v, id);
+    }
+    __syncthreads();
+    return (int)nvalid;
+  }
+  const float range = vmax - vmin;
+  const bool linear = (range > 0.0f) && isfinite(range) && isfinite(vmin) && isfinite(vmax);
+  if (!linear) {
+    const uint64_t T = block_radix_threshold<uint64_t>(
+        [&](long i) -> uint64_t {
+          float v;
+          int id;
+          return get(i, v, id) ? pack_key(v, id) : 0ull;
+        },
+        N, K, hist, scratch + 8);
+    for (long base = 0; base < N; base += blockDim.x) {
+      const long i = base + threadIdx.x;
+      float v = 0.f;
+      int id = 0;
+      const bool ok = i < N && get(i, v, id) && pack_key(v, id) >= T;
+      const uint32_t pos = warp_reserve(ok, &scratch[3]);
+      if (ok && pos < (uint32_t)K) out[pos] = pack_key(v, id);
+    }
+    __syncthreads();
+    return K;
+  }
+  const float scale = (float)kHistBins / range;
+  auto bin_of = [&](float v) -> int {
+    const int b = (int)((v - vmin) * scale);
+    return b < 0 ? 0 : (b >= kHistBins ? kHistBins - 1 : b);
+  };
+  // ---- pass 2: histogram ----
+  for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) hist[b] = 0;
+  __syncthreads();
+  for (long base = 0; base < N; base += blockDim.x) {
+    const long i = base + threadIdx.x;
+    float v = 0.f;
+    int id = 0;
+    const bool ok = i < N && get(i, v, id);
+    if (ok) atomicAdd(&hist[bin_of(v)], 1u);
+  }
+  __syncthreads();
+  // ---- threshold bin: block-wide suffix scan over the bins ----
+  {
+    // thread t owns bins [t*per, (t+1)*per); warps combine their totals
+    const int per = (kHistBins + blockDim.x - 1) / blockDim.x;
+    const int b0 = threadIdx.x * per;
+    uint32_t mine = 0;
+    for (int j = 0; j < per; ++j)
+      if (b0 + j < kHistBins) mine += hist[b0 + j];
+    uint32_t t = mine;  // inclusive suffix sum within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_down_sync(0xffffffffu, t, o);
+      if (lane + o < 32) t += v;
+    }
+    __shared__ uint32_t warp_tot[32];
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    if (lane == 0) warp_tot[warp] = t;
+    __syncthreads();
+    uint32_t above_warps = 0;
+    for (int w = warp + 1; w < nwarps; ++w) above_warps += warp_tot[w];
+    uint32_t acc = above_warps + (t - mine);  // items in bins above mine
+    for (int j = per - 1; j >= 0; --j) {
+      if (b0 + j >= kHistBins) continue;
+      const uint32_t h = hist[b0 + j];
+      if (acc < (uint32_t)K && acc + h >= (uint32_t)K) {
+        scratch[5] = (uint32_t)(b0 + j);
+        scratch[6] = acc;  // items above the threshold bin
+        scratch[7] = h;    // items in it
+      }
+      acc += h;
+    }
+  }
+  __syncthreads();
+  const int tb = (int)scratch[5];
+  const uint32_t above = scratch[6], inbin = scratch[7];
+  const uint32_t need = (uint32_t)K - above;
+  const bool fits = inbin <= (uint32_t)maybe_cap;
+  // ---- pass 3: compaction ----
+  for (long base = 0; base < N; base += blockDim.x) {
+    const long i = base + threadIdx.x;
+    float v = 0.f;
+    int id = 0;
+    const bool ok = i < N && get(i, v, id);
+    const int b = ok ? bin_of(v) : -1;
+    const bool sure = ok && b > tb;
+    const bool cand = ok && b == tb && fits;
+    const uint32_t p1 = warp_reserve(sure, &scratch[3]);
+    if (sure) out[p1] = pack_key(v, id);
+    const uint32_t p2 = warp_reserve(cand, &scratch[4]);
+    if (cand) maybe[p2] = pack_key(v, id);
+  }
+  __syncthreads();
+  if (fits) {
+    int np = 1;
+    while (np < (int)inbin) np <<= 1;
+    for (int i = (int)inbin + threadIdx.x; i < np; i += blockDim.x) maybe[i] = 0ull;
+    __syncthreads();
+    block_bitonic_sort_desc(maybe, np);
+    for (uint32_t i = threadIdx.x; i < need; i += blockDim.x) out[above + i] = maybe[i];
+    __syncthreads();
+  } else {
+    // threshold bin too large for the buffer: radix select inside it
+    auto getb = [&](long i) -> uint64_t {
+      float v;
+      int id;
+      return (get(i, v, id) && bin_of(v) == tb) ? pack_key(v, id) : 0ull;
+    };
+    const uint64_t T = block_radix_threshold<uint64_t>(getb, N, (int)need, hist, scratch + 8);
+    for (long base = 0; base < N; base += blockDim.x) {
+      const long i = base + threadIdx.x;
+      const uint64_t k = i < N ? getb(i) : 0ull;
+      const bool ok = k != 0 && k >= T;
+      const uint32_t pos = warp_reserve(ok, &scratch[3]);
+      if (ok && pos < (uint32_t)K) out[pos] = k;
+    }
+    __syncthreads();
+  }
+  return K;
+}
+
+// block_topk_hist followed by a descending sort: out[0..ret) best first,
+// out[ret..out_cap) zero. out_cap is a power of two >= K.
+template <typename GetItem>
+__device__ int block_topk_hist_sorted(GetItem get, long N, int K, uint64_t* out, int out_cap,
+                                      uint32_t* hist, uint64_t* maybe, int maybe_cap,
+                                      uint32_t* scratch) {
+  const int cnt = block_topk_hist(get, N, K, out, hist, maybe, maybe_cap, scratch);
+  for (int i = cnt + threadIdx.x; i < out_cap; i += blockDim.x) out[i] = 0ull;
+  __syncthreads();
+  block_bitonic_sort_desc(out, out_cap);
+  return cnt;
+}
+
 CEOS_DEV int next_pow2(int x) {
   int p = 1;
   while (p < x) p <<= 1;

@@ -75,7 +75,7 @@ enum QueryMode { Q_ESTIMATE = 0, Q_UNION = 1 };
 
 cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem, cudaStream_t st);
 size_t query_buckets_smem(const QueryArgs& a, int mode);
-int query_buckets_blocks_per_sm(int mode, size_t smem);
+int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem);
 cudaError_t launch_probe_select(const QueryArgs& a, cudaStream_t st);
 cudaError_t launch_dense_estimate(const QueryArgs& a, int q0, int nq_chunk, cudaStream_t st);
 cudaError_t launch_dense_select_rerank(const QueryArgs& a, int q0, int nq_chunk, cudaStream_t st);

@@ -41,32 +41,85 @@ CEOS_DEV const float* row_ptr(const QueryArgs& a, int id) {
   return a.X + r * (long)a.ldx;
 }
 
-// Sequential FMA inner product over ldx (multiple of 4) floats; padding
-// columns are zero on both sides and leave the sum unchanged.
-CEOS_DEV float dot_seq(const float* __restrict__ q, const float* __restrict__ x, int ldx) {
+// Inner product of a query with one row, in the library's canonical order:
+// the row is split into float4 chunks; lane g (0..7) of an 8-lane group
+// accumulates chunks g, g+8, g+16, ... as a sequential FMA chain
+// (s = fma(q_j, x_j, s) over the chunk's 4 elements, chunk by chunk), then the
+// 8 partial sums are combined by a butterfly (xor 4, then 2, then 1). Padding
+// columns are zero on both sides and leave every partial sum unchanged. The
+// oracle computes the same order, so scores are bit-exact between the two.
+// An 8-lane group reads 128 contiguous bytes per load, so a warp moves four
+// rows' chunks per instruction (coalesced, few outstanding requests per byte).
+CEOS_DEV float dot_g8(const float* __restrict__ q, const float* __restrict__ x, int n4, int g,
+                      bool active) {
   const float4* x4 = reinterpret_cast<const float4*>(x);
   const float4* q4 = reinterpret_cast<const float4*>(q);
   float s = 0.0f;
-  for (int j = 0; j < (ldx >> 2); ++j) {
-    const float4 xv = __ldg(x4 + j);
-    const float4 qv = q4[j];
-    s = __fmaf_rn(qv.x, xv.x, s);
-    s = __fmaf_rn(qv.y, xv.y, s);
-    s = __fmaf_rn(qv.z, xv.z, s);
-    s = __fmaf_rn(qv.w, xv.w, s);
+  if (active) {
+    int c = g;
+    for (; c + 24 < n4; c += 32) {
+      float4 xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) xv[u] = __ldcg(x4 + c + 8 * u);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 qv = q4[c + 8 * u];
+        s = __fmaf_rn(qv.x, xv[u].x, s);
+        s = __fmaf_rn(qv.y, xv[u].y, s);
+        s = __fmaf_rn(qv.z, xv[u].z, s);
+        s = __fmaf_rn(qv.w, xv[u].w, s);
+      }
+    }
+    for (; c < n4; c += 8) {
+      const float4 xv = __ldcg(x4 + c);
+      const float4 qv = q4[c];
+      s = __fmaf_rn(qv.x, xv.x, s);
+      s = __fmaf_rn(qv.y, xv.y, s);
+      s = __fmaf_rn(qv.z, xv.z, s);
+      s = __fmaf_rn(qv.w, xv.w, s);
+    }
   }
+  s = s + __shfl_xor_sync(0xffffffffu, s, 4);
+  s = s + __shfl_xor_sync(0xffffffffu, s, 2);
+  s = s + __shfl_xor_sync(0xffffffffu, s, 1);
   return s;
+}
+
+// Rerank keys[0..n) in place: each holds a candidate id (packed key); it is
+// replaced by pack_key(<q, x_id>, id). Each warp scores four rows at a time,
+// one per 8-lane group.
+template <typename RowPtr>
+CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, RowPtr row) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane & 7;
+  const int grp = lane >> 3;
+  const int warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  const int n4 = ldx >> 2;
+  for (int base = warp * 4; base < n; base += nw * 4) {
+    const int i = base + grp;
+    const bool active = i < n;
+    const int id = active ? key_id(keys[i]) : 0;
+    const float d = dot_g8(qv, active ? row(id) : qv, n4, g, active);
+    if (active && g == 0) keys[i] = pack_key(d, id);
+  }
 }
 
 CEOS_DEV int slot_id(uint64_t w) { return (int)(uint32_t)(w & 0xffffffffu); }
 CEOS_DEV float slot_val(uint64_t w) { return __uint_as_float((uint32_t)(w >> 32)); }
 
-// Find or insert `id`; returns the slot index. The capacity exceeds the
-// number of insertions, so a free slot always exists; the probe sequence is
-// still bounded by the capacity and returns -1 if it ever ran out.
+// Find or insert `id`; returns the slot index. Open addressing with double
+// hashing over a prime capacity (so every probe sequence visits every slot):
+// at the load factors a shared-memory table runs at, probe lengths have a
+// geometric tail instead of linear probing's clustered one, which matters
+// because every probed column ends at a barrier that waits for the longest
+// insertion. The capacity exceeds the number of insertions, so a free slot
+// always exists; the sequence is still bounded and returns -1 if it ran out.
 CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
-  const uint32_t h = (uint32_t)id * 0x9E3779B1u;
-  int s = (int)(((uint64_t)h * (uint32_t)cap) >> 32);
+  const uint32_t h1 = (uint32_t)id * 0x9E3779B1u;
+  const uint32_t h2 = ((uint32_t)id ^ 0x5bd1e995u) * 0x85EBCA6Bu;
+  int s = (int)(((uint64_t)h1 * (uint32_t)cap) >> 32);
+  const int step = 1 + (int)(((uint64_t)h2 * (uint32_t)(cap - 1)) >> 32);
   int* keys = reinterpret_cast<int*>(t);
   for (int probe = 0; probe < cap; ++probe) {
     const int cur = *reinterpret_cast<volatile int*>(&keys[2 * s]);
@@ -75,14 +128,17 @@ CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
       const int prev = atomicCAS(&keys[2 * s], -1, id);
       if (prev == -1 || prev == id) return s;
     }
-    s = (s + 1 == cap) ? 0 : s + 1;
+    s += step;
+    if (s >= cap) s -= cap;
   }
   return -1;
 }
 
 struct QLayout {
-  size_t qv, pkeys, probes, topk, cand, region, total;
+  size_t qv, pkeys, probes, topk, cand, hist, maybe, table, total;
 };
+
+constexpr int kMaybe = 1024;  // threshold-bin buffer of the histogram top-K
 
 __host__ __device__ inline int np2(int x) {
   int p = 1;
@@ -104,111 +160,161 @@ __host__ __device__ inline QLayout q_layout(const QueryArgs& a, int mode) {
   L.topk = o;
   o = al16(o + (size_t)np2(a.k > 0 ? a.k : 1) * 8);
   L.cand = o;
-  if (mode == Q_ESTIMATE) o = al16(o + (size_t)(a.c > 0 ? a.c : 1) * 4);
-  L.region = o;
-  size_t region = 0;
-  if (a.table_in_smem) region = (size_t)a.table_cap * 8;
-  if (mode == Q_ESTIMATE) {
-    const size_t rk = (size_t)np2(a.c > 0 ? a.c : 1) * 8;
-    if (rk > region) region = rk;
-  }
-  o = al16(o + region);
+  if (mode == Q_ESTIMATE) o = al16(o + (size_t)(a.c > 0 ? a.c : 1) * 8);
+  L.hist = o;
+  o = al16(o + (size_t)kHistBins * 4);
+  L.maybe = o;
+  o = al16(o + (size_t)kMaybe * 8);
+  L.table = o;
+  if (a.table_in_smem) o = al16(o + (size_t)a.table_cap * 8);
   L.total = o;
   return L;
 }
 
 size_t query_buckets_smem(const QueryArgs& a, int mode) { return q_layout(a, mode).total; }
 
-template <int MODE>
+constexpr int kPrefetch = 4;  // bucket columns in flight
+constexpr int kEPT = 2;       // bucket entries per thread per column on the prefetch path
+
+template <int MODE, bool SMEM_TABLE>
 __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
+  __shared__ uint32_t scratch[16];
   const QLayout Lq = q_layout(a, MODE);
   float* qv = reinterpret_cast<float*>(sm + Lq.qv);
   uint64_t* pkeys = reinterpret_cast<uint64_t*>(sm + Lq.pkeys);
   int* probes = reinterpret_cast<int*>(sm + Lq.probes);
   uint64_t* topk = reinterpret_cast<uint64_t*>(sm + Lq.topk);
-  int* cand = reinterpret_cast<int*>(sm + Lq.cand);
-  uint64_t* region = reinterpret_cast<uint64_t*>(sm + Lq.region);
-  uint64_t* table = a.table_in_smem ? region : a.gtable + (long)blockIdx.x * a.table_cap;
+  uint64_t* cand = reinterpret_cast<uint64_t*>(sm + Lq.cand);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm + Lq.hist);
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(sm + Lq.maybe);
+  // The table pointer's address space is fixed per instantiation so that
+  // shared-memory tables get shared (not generic) loads and atomics.
+  uint64_t* table = SMEM_TABLE ? reinterpret_cast<uint64_t*>(sm + Lq.table)
+                               : a.gtable + (long)blockIdx.x * a.table_cap;
   const int cap = a.table_cap;
   const int s_cap = np2(a.s > 0 ? a.s : 1);
   const int k_cap = np2(a.k > 0 ? a.k : 1);
+  const unsigned long npts = (unsigned long)a.n_points;
 
   for (int q = blockIdx.x; q < a.nq; q += gridDim.x) {
     for (int j = threadIdx.x; j < a.ldx; j += blockDim.x) qv[j] = a.Q[(long)q * a.ldx + j];
-    // ---- 1. probes ----
+    // ---- 1. probes: top-s |projection|, consumed worst first ----
     const float* qp = a.qproj + (long)q * a.C;
-    const int ns = block_topk_sorted([&](long i) { return pack_key(abs_ref(qp[i]), (int)i); },
-                                     (long)a.C, a.s, pkeys, s_cap, hist, scratch);
+    const int ns = block_topk_hist_sorted(
+        [&](long i, float& v, int& id) {
+          v = abs_ref(qp[i]);
+          id = (int)i;
+          return true;
+        },
+        (long)a.C, a.s, pkeys, s_cap, hist, maybe, kMaybe, scratch);
     for (int j = threadIdx.x; j < ns; j += blockDim.x) {
       const int col = key_id(pkeys[ns - 1 - j]);
       probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
     }
     for (int i = threadIdx.x; i < cap; i += blockDim.x) table[i] = kEmptySlot;
     __syncthreads();
-    // ---- 2. estimate / union ----
-    for (int j = 0; j < ns; ++j) {
-      const int tag = probes[j];
-      const int col = (tag < 0 ? -tag : tag) - 1;
-      const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m;
-      for (int e = threadIdx.x; e < a.p; e += blockDim.x) {
-        const int id = __ldg(a.bids + base + e);
-        // streamCEOs can keep stale bucket rows whose id is no longer a live
-        // point; they are skipped (the reference reads out of range there).
-        if ((unsigned)id >= (unsigned long)a.n_points) continue;
-        const int sl = table_slot(table, cap, id);
-        if (sl < 0) continue;
-        if (MODE == Q_ESTIMATE) {
-          const float v = __ldg(a.bvals + base + e);
-          atomicAdd(reinterpret_cast<float*>(&table[sl]) + 1, v);
+    // ---- 2. ordered accumulation / union of the probed bucket prefixes ----
+    auto insert = [&](int id, float v) {
+      if ((unsigned long)(unsigned)id >= npts) return;  // stale streamCEOs row
+      const int sl = table_slot(table, cap, id);
+      if (sl < 0) return;
+      if (MODE == Q_ESTIMATE) atomicAdd(reinterpret_cast<float*>(&table[sl]) + 1, v);
+    };
+    if (a.p <= kEPT * (int)blockDim.x) {
+      int pid[kPrefetch][kEPT];
+      float pv[kPrefetch][kEPT];
+      auto load = [&](int j, int (&ids)[kEPT], float (&vs)[kEPT]) {
+        const int tag = probes[j];
+        const int col = (tag < 0 ? -tag : tag) - 1;
+        const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m;
+#pragma unroll
+        for (int t = 0; t < kEPT; ++t) {
+          const int e = threadIdx.x + t * blockDim.x;
+          ids[t] = -1;
+          vs[t] = 0.0f;
+          if (e < a.p) {
+            ids[t] = __ldg(a.bids + base + e);
+            if (MODE == Q_ESTIMATE) vs[t] = __ldg(a.bvals + base + e);
+          }
+        }
+      };
+#pragma unroll
+      for (int u = 0; u < kPrefetch; ++u)
+        if (u < ns) load(u, pid[u], pv[u]);
+      for (int j0 = 0; j0 < ns; j0 += kPrefetch) {
+#pragma unroll
+        for (int u = 0; u < kPrefetch; ++u) {
+          const int j = j0 + u;
+          if (j < ns) {
+#pragma unroll
+            for (int t = 0; t < kEPT; ++t)
+              if (pid[u][t] != -1) insert(pid[u][t], pv[u][t]);
+            if (j + kPrefetch < ns) load(j + kPrefetch, pid[u], pv[u]);
+            if (MODE == Q_ESTIMATE) __syncthreads();
+          }
         }
       }
-      if (MODE == Q_ESTIMATE) __syncthreads();
+    } else {
+      for (int j = 0; j < ns; ++j) {
+        const int tag = probes[j];
+        const int col = (tag < 0 ? -tag : tag) - 1;
+        const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m;
+        for (int e = threadIdx.x; e < a.p; e += blockDim.x)
+          insert(__ldg(a.bids + base + e), MODE == Q_ESTIMATE ? __ldg(a.bvals + base + e) : 0.0f);
+        if (MODE == Q_ESTIMATE) __syncthreads();
+      }
     }
     __syncthreads();
     int nres;
     if (MODE == Q_ESTIMATE) {
-      // ---- 3. top-c candidates ----
-      auto getc = [&](long i) -> uint64_t {
-        const uint64_t w = *reinterpret_cast<volatile uint64_t*>(&table[i]);
-        const int id = slot_id(w);
-        return id < 0 ? 0ull : pack_key(slot_val(w), id);
-      };
-      const uint64_t T = block_radix_threshold<uint64_t>(getc, (long)cap, a.c, hist, scratch);
-      if (threadIdx.x == 0) scratch[5] = 0;
+      // ---- 3. top-c candidates by estimate ----
+      const int nc = block_topk_hist(
+          [&](long i, float& v, int& id) {
+            const uint64_t w = *reinterpret_cast<volatile uint64_t*>(&table[i]);
+            id = slot_id(w);
+            v = slot_val(w);
+            return id >= 0;
+          },
+          (long)cap, a.c, cand, hist, maybe, kMaybe, scratch);
+      // ---- 4. exact rerank, in place ----
+      rerank_inplace(cand, nc, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
       __syncthreads();
-      for (int i = threadIdx.x; i < cap; i += blockDim.x) {
-        const uint64_t k = getc(i);
-        if (k != 0 && k >= T) {
-          const uint32_t pos = atomicAdd(&scratch[5], 1u);
-          if (pos < (uint32_t)a.c) cand[pos] = key_id(k);
+      nres = block_topk_hist_sorted(
+          [&](long i, float& v, int& id) {
+            const uint64_t k = cand[i];
+            v = key_val(k);
+            id = key_id(k);
+            return true;
+          },
+          (long)nc, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+    } else {
+      // ---- union rerank in place over the table slots ----
+      {
+        const int lane = threadIdx.x & 31;
+        const int g = lane & 7;
+        const int grp = lane >> 3;
+        const int warp = threadIdx.x >> 5;
+        const int nw = blockDim.x >> 5;
+        for (int base = warp * 4; base < cap; base += nw * 4) {
+          const int i = base + grp;
+          const uint64_t w = i < cap ? (uint64_t)(*reinterpret_cast<volatile uint64_t*>(&table[i])) : (uint64_t)kEmptySlot;
+          const int id = slot_id(w);
+          const bool active = id >= 0;
+          const float d = dot_g8(qv, active ? row_ptr(a, id) : qv, a.ldx >> 2, g, active);
+          __syncwarp();
+          if (i < cap && g == 0) table[i] = active ? pack_key(d, id) : 0ull;
         }
       }
       __syncthreads();
-      const int nc = (int)min(scratch[5], (uint32_t)(a.c > 0 ? a.c : 0));
-      __syncthreads();
-      // ---- 4. rerank ----
-      uint64_t* rk = region;
-      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-        const int id = cand[i];
-        rk[i] = pack_key(dot_seq(qv, row_ptr(a, id), a.ldx), id);
-      }
-      __syncthreads();
-      nres = block_topk_sorted([&](long i) { return rk[i]; }, (long)nc, a.k, topk, k_cap, hist,
-                               scratch);
-    } else {
-      // ---- union rerank in place over the table slots ----
-      for (int i = threadIdx.x; i < cap; i += blockDim.x) {
-        const uint64_t w = *reinterpret_cast<volatile uint64_t*>(&table[i]);
-        const int id = slot_id(w);
-        table[i] = id < 0 ? 0ull : pack_key(dot_seq(qv, row_ptr(a, id), a.ldx), id);
-      }
-      __syncthreads();
-      nres = block_topk_sorted(
-          [&](long i) { return *reinterpret_cast<volatile uint64_t*>(&table[i]); }, (long)cap, a.k,
-          topk, k_cap, hist, scratch);
+      nres = block_topk_hist_sorted(
+          [&](long i, float& v, int& id) {
+            const uint64_t k = *reinterpret_cast<volatile uint64_t*>(&table[i]);
+            v = key_val(k);
+            id = key_id(k);
+            return k != 0ull;
+          },
+          (long)cap, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
     }
     for (int i = threadIdx.x; i < a.k; i += blockDim.x) {
       a.out_ids[(long)q * a.k + i] = i < nres ? key_id(topk[i]) : 0;
@@ -218,38 +324,33 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
   }
 }
 
-cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem,
-                                 cudaStream_t st) {
-  if (a.nq <= 0) return cudaSuccess;
-  cudaError_t e;
-  if (mode == Q_ESTIMATE) {
-    e = cudaFuncSetAttribute(k_query_buckets<Q_ESTIMATE>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k_query_buckets<Q_ESTIMATE><<<grid, kQueryThreads, smem, st>>>(a);
-  } else {
-    e = cudaFuncSetAttribute(k_query_buckets<Q_UNION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) return e;
-    k_query_buckets<Q_UNION><<<grid, kQueryThreads, smem, st>>>(a);
-  }
+template <int MODE, bool SM>
+static cudaError_t launch_qb(const QueryArgs& a, int grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_query_buckets<MODE, SM>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_query_buckets<MODE, SM><<<grid, kQueryThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
-int query_buckets_blocks_per_sm(int mode, size_t smem) {
+cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem,
+                                 cudaStream_t st) {
+  if (a.nq <= 0) return cudaSuccess;
+  if (mode == Q_ESTIMATE)
+    return a.table_in_smem ? launch_qb<Q_ESTIMATE, true>(a, grid, smem, st)
+                           : launch_qb<Q_ESTIMATE, false>(a, grid, smem, st);
+  return a.table_in_smem ? launch_qb<Q_UNION, true>(a, grid, smem, st)
+                         : launch_qb<Q_UNION, false>(a, grid, smem, st);
+}
+
+template <int MODE, bool SM>
+static int occ_qb(size_t smem) {
   int n = 0;
-  cudaError_t e;
-  if (mode == Q_ESTIMATE) {
-    e = cudaFuncSetAttribute(k_query_buckets<Q_ESTIMATE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_buckets<Q_ESTIMATE>, kQueryThreads, smem);
-  } else {
-    e = cudaFuncSetAttribute(k_query_buckets<Q_UNION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_buckets<Q_UNION>, kQueryThreads, smem);
-  }
+  cudaError_t e = cudaFuncSetAttribute(k_query_buckets<MODE, SM>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_buckets<MODE, SM>, kQueryThreads,
+                                                      smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -257,18 +358,30 @@ int query_buckets_blocks_per_sm(int mode, size_t smem) {
   return n;
 }
 
+int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem) {
+  if (mode == Q_ESTIMATE) return table_in_smem ? occ_qb<Q_ESTIMATE, true>(smem) : occ_qb<Q_ESTIMATE, false>(smem);
+  return table_in_smem ? occ_qb<Q_UNION, true>(smem) : occ_qb<Q_UNION, false>(smem);
+}
+
 // ---------------------------------------------------------------------------
 // Dense CEOs-Est.
 
 __global__ void __launch_bounds__(256) k_probe_select(QueryArgs a) {
-  extern __shared__ __align__(16) uint64_t pk[];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ uint32_t scratch[16];
+  const int s_cap = np2(a.s > 0 ? a.s : 1);
+  uint64_t* pk = reinterpret_cast<uint64_t*>(sm);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm + (size_t)s_cap * 8);
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(sm + (size_t)s_cap * 8 + (size_t)kHistBins * 4);
   const int q = blockIdx.x;
   const float* qp = a.qproj + (long)q * a.C;
-  const int s_cap = np2(a.s > 0 ? a.s : 1);
-  const int ns = block_topk_sorted([&](long i) { return pack_key(abs_ref(qp[i]), (int)i); },
-                                   (long)a.C, a.s, pk, s_cap, hist, scratch);
+  const int ns = block_topk_hist_sorted(
+      [&](long i, float& v, int& id) {
+        v = abs_ref(qp[i]);
+        id = (int)i;
+        return true;
+      },
+      (long)a.C, a.s, pk, s_cap, hist, maybe, kMaybe, scratch);
   for (int j = threadIdx.x; j < a.s; j += blockDim.x) {
     int tag = 0;
     if (j < ns) {
@@ -281,7 +394,10 @@ __global__ void __launch_bounds__(256) k_probe_select(QueryArgs a) {
 
 cudaError_t launch_probe_select(const QueryArgs& a, cudaStream_t st) {
   if (a.nq <= 0 || a.s <= 0) return cudaSuccess;
-  const size_t smem = (size_t)np2(a.s) * 8;
+  const size_t smem = (size_t)np2(a.s) * 8 + (size_t)kHistBins * 4 + (size_t)kMaybe * 8;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_probe_select, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   k_probe_select<<<a.nq, 256, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -320,39 +436,33 @@ cudaError_t launch_dense_estimate(const QueryArgs& a, int q0, int nq_chunk, cuda
 // Top-c over all n estimates of one query, then the exact rerank and top-k.
 __global__ void __launch_bounds__(kQueryThreads) k_dense_select_rerank(QueryArgs a, int q0) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
+  __shared__ uint32_t scratch[16];
   const int qi = blockIdx.x;
   const int q = q0 + qi;
   const int k_cap = np2(a.k > 0 ? a.k : 1);
-  const int c_cap = np2(a.c > 0 ? a.c : 1);
   float* qv = reinterpret_cast<float*>(sm);
   uint64_t* topk = reinterpret_cast<uint64_t*>(sm + al16((size_t)a.ldx * 4));
-  uint64_t* rk = topk + k_cap;
-  int* cand = reinterpret_cast<int*>(rk + c_cap);
+  uint64_t* cand = topk + k_cap;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(cand + (a.c > 0 ? a.c : 1));
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(hist + kHistBins);
   for (int j = threadIdx.x; j < a.ldx; j += blockDim.x) qv[j] = a.Q[(long)q * a.ldx + j];
   const float* est = a.est + (long)qi * a.n_points;
-  auto gete = [&](long i) { return pack_key(est[i], (int)i); };
-  const uint64_t T = block_radix_threshold<uint64_t>(gete, a.n_points, a.c, hist, scratch);
-  if (threadIdx.x == 0) scratch[5] = 0;
+  const int nc = block_topk_hist(
+      [&](long i, float& v, int& id) {
+        v = est[i];
+        id = (int)i;
+        return true;
+      },
+      a.n_points, a.c, cand, hist, maybe, kMaybe, scratch);
+  rerank_inplace(cand, nc, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
   __syncthreads();
-  for (long i = threadIdx.x; i < a.n_points; i += blockDim.x) {
-    const uint64_t k = gete(i);
-    if (k >= T) {
-      const uint32_t pos = atomicAdd(&scratch[5], 1u);
-      if (pos < (uint32_t)a.c) cand[pos] = (int)i;
-    }
-  }
-  __syncthreads();
-  const int nc = (int)min(scratch[5], (uint32_t)(a.c > 0 ? a.c : 0));
-  __syncthreads();
-  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-    const int id = cand[i];
-    rk[i] = pack_key(dot_seq(qv, row_ptr(a, id), a.ldx), id);
-  }
-  __syncthreads();
-  const int nres =
-      block_topk_sorted([&](long i) { return rk[i]; }, (long)nc, a.k, topk, k_cap, hist, scratch);
+  const int nres = block_topk_hist_sorted(
+      [&](long i, float& v, int& id) {
+        v = key_val(cand[i]);
+        id = key_id(cand[i]);
+        return true;
+      },
+      (long)nc, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
   for (int i = threadIdx.x; i < a.k; i += blockDim.x) {
     a.out_ids[(long)q * a.k + i] = i < nres ? key_id(topk[i]) : 0;
     a.out_d[(long)q * a.k + i] = i < nres ? key_val(topk[i]) : 0.0f;
@@ -362,9 +472,8 @@ __global__ void __launch_bounds__(kQueryThreads) k_dense_select_rerank(QueryArgs
 cudaError_t launch_dense_select_rerank(const QueryArgs& a, int q0, int nq_chunk, cudaStream_t st) {
   if (nq_chunk <= 0) return cudaSuccess;
   const int k_cap = np2(a.k > 0 ? a.k : 1);
-  const int c_cap = np2(a.c > 0 ? a.c : 1);
-  const size_t smem = al16((size_t)a.ldx * 4) + (size_t)k_cap * 8 + (size_t)c_cap * 8 +
-                      (size_t)(a.c > 0 ? a.c : 1) * 4;
+  const size_t smem = al16((size_t)a.ldx * 4) + (size_t)k_cap * 8 + (size_t)(a.c > 0 ? a.c : 1) * 8 +
+                      (size_t)kHistBins * 4 + (size_t)kMaybe * 8;
   cudaError_t e = cudaFuncSetAttribute(k_dense_select_rerank,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -11,9 +11,9 @@
 //   2. the full projection runs in PROJ_EMIT mode, appending every value whose
 //      key clears a threshold to that column end's candidate list.
 //   3. k_finish_buckets picks the exact top-m of each candidate list (a
-//      block-wide radix select on packed (value, id) keys, then a bitonic
-//      sort) and writes the bucket best first, as the reference pops its heap
-//      into rows m-1 .. 0.
+//      block-wide value-histogram select on packed (value, id) keys, then a
+//      bitonic sort) and writes the bucket best first, as the reference pops
+//      its heap into rows m-1 .. 0.
 // A column end whose list came out short (< m) or overflowed is flagged; the
 // host then dumps those full columns and k_exact_buckets selects them exactly.
 #include "kernels.h"
@@ -43,12 +43,24 @@ cudaError_t launch_sample_thresholds(const float* samp, long S, int C, int rank,
   return cudaGetLastError();
 }
 
+// Dynamic shared memory of the per-column-end selections: sorted output
+// (next_pow2(K) keys), the value histogram and the threshold-bin buffer.
+constexpr int kSelMaybe = 1024;
+static size_t sel_smem(int K) {
+  int cap = 1;
+  while (cap < K) cap <<= 1;
+  return (size_t)cap * 8 + (size_t)kHistBins * 4 + (size_t)kSelMaybe * 8;
+}
+
 __global__ void __launch_bounds__(256) k_finish_buckets(const uint64_t* cand, const unsigned* cnt,
                                                        int cap, int m, int* bids, float* bvals,
                                                        unsigned* fail) {
-  extern __shared__ __align__(16) uint64_t s_out[];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ uint32_t scratch[16];
+  const int out_cap = next_pow2(m);
+  uint64_t* s_out = reinterpret_cast<uint64_t*>(sm);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm + (size_t)out_cap * 8);
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(hist + kHistBins);
   const long ce = blockIdx.x;  // 2 * column + end
   const unsigned n = cnt[ce];
   if (n < (unsigned)m || n > (unsigned)cap) {
@@ -56,8 +68,14 @@ __global__ void __launch_bounds__(256) k_finish_buckets(const uint64_t* cand, co
     return;
   }
   const uint64_t* list = cand + ce * cap;
-  const int out_cap = next_pow2(m);
-  block_topk_sorted([&](long i) { return list[i]; }, (long)n, m, s_out, out_cap, hist, scratch);
+  block_topk_hist_sorted(
+      [&](long i, float& v, int& id) {
+        const uint64_t k = list[i];
+        v = key_val(k);
+        id = key_id(k);
+        return true;
+      },
+      (long)n, m, s_out, out_cap, hist, maybe, kSelMaybe, scratch);
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const uint64_t k = s_out[i];
     bids[ce * m + i] = key_id(k);
@@ -67,9 +85,7 @@ __global__ void __launch_bounds__(256) k_finish_buckets(const uint64_t* cand, co
 
 cudaError_t launch_finish_buckets(const uint64_t* cand, const unsigned* cnt, int cap, int C, int m,
                                   int* bids, float* bvals, unsigned* fail, cudaStream_t st) {
-  int out_cap = 1;
-  while (out_cap < m) out_cap <<= 1;
-  const size_t smem = (size_t)out_cap * 8;
+  const size_t smem = sel_smem(m);
   cudaError_t e =
       cudaFuncSetAttribute(k_finish_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -81,22 +97,25 @@ cudaError_t launch_finish_buckets(const uint64_t* cand, const unsigned* cnt, int
 __global__ void __launch_bounds__(512) k_exact_buckets(const float* vals, long n, long ld,
                                                       const int* col_of_slot, const unsigned* fail,
                                                       int m, int* bids, float* bvals) {
-  extern __shared__ __align__(16) uint64_t s_out[];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ uint32_t scratch[16];
+  const int out_cap = next_pow2(m);
+  uint64_t* s_out = reinterpret_cast<uint64_t*>(sm);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm + (size_t)out_cap * 8);
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(hist + kHistBins);
   const int slot = blockIdx.x >> 1;
   const int end = blockIdx.x & 1;
   const int col = col_of_slot[slot];
   const long ce = 2L * col + end;
   if (!fail[ce]) return;
   const float* v = vals + (long)slot * ld;
-  const int out_cap = next_pow2(m);
-  if (end == 0)
-    block_topk_sorted([&](long i) { return pack_key(v[i], (int)i); }, n, m, s_out, out_cap, hist,
-                      scratch);
-  else
-    block_topk_sorted([&](long i) { return pack_key(-v[i], (int)i); }, n, m, s_out, out_cap, hist,
-                      scratch);
+  block_topk_hist_sorted(
+      [&](long i, float& x, int& id) {
+        x = end ? -v[i] : v[i];
+        id = (int)i;
+        return true;
+      },
+      n, m, s_out, out_cap, hist, maybe, kSelMaybe, scratch);
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const uint64_t k = s_out[i];
     bids[ce * m + i] = key_id(k);
@@ -107,9 +126,7 @@ __global__ void __launch_bounds__(512) k_exact_buckets(const float* vals, long n
 cudaError_t launch_exact_buckets(const float* vals, long n, long ld, int n_slots,
                                  const int* col_of_slot, const unsigned* fail, int m, int* bids,
                                  float* bvals, cudaStream_t st) {
-  int out_cap = 1;
-  while (out_cap < m) out_cap <<= 1;
-  const size_t smem = (size_t)out_cap * 8;
+  const size_t smem = sel_smem(m);
   cudaError_t e =
       cudaFuncSetAttribute(k_exact_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

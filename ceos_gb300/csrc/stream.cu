@@ -16,29 +16,36 @@
 
 namespace ceos {
 
+constexpr int kMergeMaybe = 1024;
+
 __global__ void __launch_bounds__(512) k_stream_merge(int m, const float* newP, long b, long cur,
                                                      int n_del, int* bids, float* bvals) {
-  extern __shared__ __align__(16) uint64_t s_out[];
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ uint32_t scratch[16];
+  const int out_cap = next_pow2(2 * m);
+  uint64_t* s_out = reinterpret_cast<uint64_t*>(sm);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm + (size_t)out_cap * 8);
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(hist + kHistBins);
   const long ce = blockIdx.x;
   const int col = (int)(ce >> 1);
   const int end = (int)(ce & 1);
   int* ids = bids + ce * m;
   float* vals = bvals + ce * m;
   const float* np = newP + (long)col * b;
-  auto get = [&](long i) -> uint64_t {
+  auto get = [&](long i, float& v, int& id) -> bool {
     if (i < m) {
-      const int id = ids[i];
-      return id >= n_del ? pack_key(vals[i], id) : 0ull;
+      id = ids[i];
+      v = vals[i];
+      return id >= n_del;
     }
     const long t = i - m;
-    const float v = np[t];
-    return pack_key(end ? -v : v, (int)(cur + t));
+    v = end ? -np[t] : np[t];
+    id = (int)(cur + t);
+    return true;
   };
-  const int out_cap = next_pow2(2 * m);
-  const int cnt = block_topk_sorted(get, (long)m + b, m, s_out, out_cap, hist, scratch);
-  // block_topk_sorted ends with a barrier, so every read of ids/vals is done.
+  const int cnt = block_topk_hist_sorted(get, (long)m + b, m, s_out, out_cap, hist, maybe,
+                                         kMergeMaybe, scratch);
+  // the sort ends with a barrier, so every read of ids/vals is done
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
     const uint64_t k = s_out[i];
     ids[i] = key_id(k) - n_del;
@@ -50,7 +57,7 @@ cudaError_t launch_stream_merge(int C, int m, const float* newP, long b, long cu
                                 int* bids, float* bvals, cudaStream_t st) {
   int out_cap = 1;
   while (out_cap < 2 * m) out_cap <<= 1;
-  const size_t smem = (size_t)out_cap * 8;
+  const size_t smem = (size_t)out_cap * 8 + (size_t)kHistBins * 4 + (size_t)kMergeMaybe * 8;
   cudaError_t e =
       cudaFuncSetAttribute(k_stream_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

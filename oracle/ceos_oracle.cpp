@@ -28,9 +28,10 @@
 //    +0), then smaller id wins. The reference (src/Header.h:53-80) compares
 //    the value only, so which of several exactly tied items it keeps depends
 //    on heap layout / robin_map iteration order.
-//  * The rerank inner product is a sequential fused multiply-add chain
-//    (std::fma over j = 0..d-1). The reference uses Eigen's vectorised dot,
-//    whose association differs at the ulp level.
+//  * The rerank inner product uses one fixed association (8 strided fused
+//    multiply-add chains over float4 chunks, then a butterfly; see dot_fma),
+//    the one the GPU kernels compute. The reference uses Eigen's vectorised
+//    dot, whose association differs at the ulp level.
 //  * Per-query estimates are kept in an ordered map instead of tsl::robin_map;
 //    the accumulation order per point (probe pop order) is the reference's.
 //  * Parameter errors return a negative status instead of exit(1); asking for
@@ -222,11 +223,29 @@ static void project_rows(const float* X, long n, int d, int F, int D, int R,
   }
 }
 
-// Sequential fused multiply-add inner product (the rerank score).
+// Rerank score in the GPU library's canonical order: the row is split into
+// float4 chunks; partial sum g (g = 0..7) is a sequential fused multiply-add
+// chain over chunks g, g+8, g+16, ... (4 elements each, elements past d
+// count as zero), and the 8 partial sums are combined as a butterfly (pairs
+// g, g^4; then g, g^2; then g, g^1), the value lane 0 of an 8-lane group ends
+// with.
 static inline float dot_fma(const float* a, const float* b, int d) {
-  float s = 0.0f;
-  for (int j = 0; j < d; ++j) s = std::fma(a[j], b[j], s);
-  return s;
+  const int n4 = (d + 3) / 4;
+  float p[8];
+  for (int g = 0; g < 8; ++g) {
+    float s = 0.0f;
+    for (int c = g; c < n4; c += 8)
+      for (int e = 0; e < 4; ++e) {
+        const int j = 4 * c + e;
+        if (j < d) s = std::fma(a[j], b[j], s);
+      }
+    p[g] = s;
+  }
+  float t[8];
+  for (int g = 0; g < 8; ++g) t[g] = p[g] + p[g ^ 4];
+  for (int g = 0; g < 8; ++g) p[g] = t[g] + t[g ^ 2];
+  for (int g = 0; g < 8; ++g) t[g] = p[g] + p[g ^ 1];
+  return t[0];
 }
 
 // Two-ended top-m of one projection column, written as the reference lays
