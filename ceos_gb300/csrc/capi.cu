@@ -452,6 +452,7 @@ struct Core {
     q.bids = dBids.as<int>();
     q.bvals = dBvals.as<float>();
     q.P = dP.as<float>();
+    q.distinct_ids = built == B_STREAM ? 0 : 1;
     return q;
   }
 
@@ -1147,6 +1148,7 @@ extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float*
   q.n_points = c.n_rows;
   q.bids = c.dBids.as<int>();
   q.bvals = c.dBvals.as<float>();
+  q.distinct_ids = 1;
   q.out_ids = d_ids;
   q.out_d = d_dists;
   const long tc = table_capacity(c.s, c.p);

@@ -54,26 +54,48 @@ CEOS_DEV int line_elem(int line, int e, int o, int b) {
   return low | (e << o) | (high << (o + b));
 }
 
+// Two butterflies at once: (a0, c0) and (a1, c1) become (a0+c0, a0-c0) and
+// (a1+c1, a1-c1), as packed f32x2 adds/subtracts (two IEEE round-to-nearest
+// operations each, so the results are those of the scalar form).
+CEOS_DEV void bfly2(float& a0, float& a1, float& c0, float& c1) {
+  unsigned long long A, C, S, D;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(A) : "f"(a0), "f"(a1));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(C) : "f"(c0), "f"(c1));
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(S) : "l"(A), "l"(C));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(D) : "l"(A), "l"(C));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a0), "=f"(a1) : "l"(S));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(c0), "=f"(c1) : "l"(D));
+}
+
 // Butterfly stages [0, b) of a register line (stage s pairs e and e + 2^s).
+// Stages with a stride of 2 or more pair up adjacent butterflies into f32x2
+// operations on register pairs (e, e+1) and (e+h, e+h+1).
 template <int B>
 CEOS_DEV void reg_stages(float (&v)[1 << B]) {
+  constexpr int E = 1 << B;
 #pragma unroll
   for (int s = 0; s < B; ++s) {
     const int h = 1 << s;
+    if (h == 1) {
 #pragma unroll
-    for (int e = 0; e < (1 << B); ++e) {
-      if ((e & h) == 0) {
-        const float a = v[e], c = v[e + h];
+      for (int e = 0; e < E; e += 2) {
+        const float a = v[e], c = v[e + 1];
         v[e] = a + c;
-        v[e + h] = a - c;
+        v[e + 1] = a - c;
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; e += 2 * h) {
+#pragma unroll
+        for (int k = 0; k < h; k += 2) bfly2(v[e + k], v[e + k + 1], v[e + k + h], v[e + k + 1 + h]);
       }
     }
   }
 }
 
 // Phase p >= 1 of a round: bits [off(p), off(p) + bits(p)) in registers.
-template <int L, int p, bool KEEP_LAST>
-CEOS_DEV void fwht_phase(float* dst, int lane, float (*out)[FwhtCfg<L>::Emax]) {
+template <int L, int p>
+CEOS_DEV void fwht_phase(float* dst, int lane) {
   using Cfg = FwhtCfg<L>;
   constexpr int o = Cfg::off(p);
   constexpr int B = Cfg::bits(p);
@@ -90,26 +112,20 @@ CEOS_DEV void fwht_phase(float* dst, int lane, float (*out)[FwhtCfg<L>::Emax]) {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = d[padj(line_elem(line, e, o, B))];
     reg_stages<B>(v);
-    if (KEEP_LAST && p == Cfg::P - 1) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) out[t][e] = v[e];
-    } else {
-#pragma unroll
-      for (int e = 0; e < E; ++e) d[padj(line_elem(line, e, o, B))] = v[e];
-    }
+    for (int e = 0; e < E; ++e) d[padj(line_elem(line, e, o, B))] = v[e];
   }
-  if constexpr (p + 1 < Cfg::P) fwht_phase<L, p + 1, KEEP_LAST>(dst, lane, out);
+  if constexpr (p + 1 < Cfg::P) fwht_phase<L, p + 1>(dst, lane);
 }
 
 // One full round (sign flip + FWHT) on the warp's V vectors.
 //  src: smem base the round reads from (V vectors, stride Vstride)
 //  dst: smem base it writes to (may equal src)
 //  sw : 32-bit sign words of this round (bit j set => multiply by +1)
-// If KEEP_LAST, the last phase's register lines are left in `out`
-// (tasks(P-1) lines of E(P-1) floats) and are NOT stored to dst.
-template <int L, bool KEEP_LAST>
-CEOS_DEV void fwht_round(const float* src, float* dst, const uint32_t* sw, int lane,
-                         float (*out)[FwhtCfg<L>::Emax]) {
+// Phase 0 covers the lowest index bits, so its lines are contiguous chunks
+// and move as float4 when they are at least 4 elements long.
+template <int L>
+CEOS_DEV void fwht_round(const float* src, float* dst, const uint32_t* sw, int lane) {
   using Cfg = FwhtCfg<L>;
   constexpr int B = Cfg::bits(0);
   constexpr int E = 1 << B;
@@ -120,41 +136,38 @@ CEOS_DEV void fwht_round(const float* src, float* dst, const uint32_t* sw, int l
     const int vec = task / lines0;
     const int line = task % lines0;
     const int j0 = line * E;
-    const float* s = src + vec * Cfg::Vstride;
-    float* d = dst + vec * Cfg::Vstride;
-    const uint32_t word = sw[j0 >> 5] >> (j0 & 31);
+    const float* s = src + vec * Cfg::Vstride + padj(j0);
+    float* d = dst + vec * Cfg::Vstride + padj(j0);
+    const uint32_t nword = ~(sw[j0 >> 5] >> (j0 & 31));  // bit e set => flip
     float v[E];
+    if constexpr (E >= 4) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const uint32_t flip = ((word >> e) & 1u) ? 0u : 0x80000000u;
-      v[e] = __uint_as_float(__float_as_uint(s[padj(j0 + e)]) ^ flip);
-    }
-    reg_stages<B>(v);
-    if (KEEP_LAST && Cfg::P == 1) {
-#pragma unroll
-      for (int e = 0; e < E; ++e) out[t][e] = v[e];
+      for (int k = 0; k < E / 4; ++k) {
+        const float4 q = reinterpret_cast<const float4*>(s)[k];
+        v[4 * k] = q.x;
+        v[4 * k + 1] = q.y;
+        v[4 * k + 2] = q.z;
+        v[4 * k + 3] = q.w;
+      }
     } else {
 #pragma unroll
-      for (int e = 0; e < E; ++e) d[padj(j0 + e)] = v[e];
+      for (int e = 0; e < E; ++e) v[e] = s[e];
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      v[e] = __uint_as_float(__float_as_uint(v[e]) ^ ((nword << (31 - e)) & 0x80000000u));
+    reg_stages<B>(v);
+    if constexpr (E >= 4) {
+#pragma unroll
+      for (int k = 0; k < E / 4; ++k)
+        reinterpret_cast<float4*>(d)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) d[e] = v[e];
     }
   }
-  if constexpr (Cfg::P > 1) fwht_phase<L, 1, KEEP_LAST>(dst, lane, out);
+  if constexpr (Cfg::P > 1) fwht_phase<L, 1>(dst, lane);
   __syncwarp();
-}
-
-// Map (task t of the last phase, register e) to the element index j and the
-// vector slot within the warp.
-template <int L>
-CEOS_DEV void last_phase_index(int lane, int t, int e, int& vec, int& j) {
-  using Cfg = FwhtCfg<L>;
-  constexpr int p = Cfg::P - 1;
-  const int o = Cfg::off(p);
-  const int B = Cfg::bits(p);
-  const int lines = Cfg::F / (1 << B);
-  const int task = lane + 32 * t;
-  vec = task / lines;
-  const int line = task % lines;
-  j = line_elem(line, e, o, B);
 }
 
 }  // namespace ceos

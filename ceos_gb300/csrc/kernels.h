@@ -59,6 +59,9 @@ struct QueryArgs {
   const float* P = nullptr;     // dense CEOs-Est projections [C][n]
   int* out_ids = nullptr;
   float* out_d = nullptr;
+  // 1 when every bucket column holds distinct ids (CEOs / coCEOs indexes); a
+  // streamCEOs index can keep stale rows that repeat an id within a column
+  int distinct_ids = 0;
   // hash table (estimate / union), in shared memory when table_in_smem
   int table_cap = 0;
   int table_in_smem = 0;

@@ -68,21 +68,19 @@ __global__ void __launch_bounds__(256) k_project(ProjArgs a) {
     }
     __syncwarp();
     for (int r = 0; r < a.R; ++r) {
-      float out[Cfg::tasks(Cfg::P - 1)][Cfg::Emax];
       const uint32_t* sw = s_signs + (size_t)r * 3 * words;
-      fwht_round<L, false>(xbuf, wbuf, sw, lane, nullptr);
-      fwht_round<L, false>(wbuf, wbuf, sw + words, lane, nullptr);
-      fwht_round<L, true>(wbuf, wbuf, sw + 2 * words, lane, out);
-      constexpr int B = Cfg::bits(Cfg::P - 1);
-#pragma unroll
-      for (int t = 0; t < Cfg::tasks(Cfg::P - 1); ++t) {
-#pragma unroll
-        for (int e = 0; e < (1 << B); ++e) {
-          int vec, j;
-          last_phase_index<L>(lane, t, e, vec, j);
-          const long row = row0 + vec;
-          if (j >= a.D || row >= a.n_rows) continue;
-          const float v = out[t][e];
+#pragma unroll 1
+      for (int i = 0; i < 3; ++i) fwht_round<L>(i == 0 ? xbuf : wbuf, wbuf, sw + i * words, lane);
+      // outputs j < D of each vector, consecutive lanes on consecutive columns
+#pragma unroll 1
+      for (int vec = 0; vec < Cfg::V; ++vec) {
+        const long row = row0 + vec;
+        if (row >= a.n_rows) break;
+        const float* w = wbuf + vec * Cfg::Vstride;
+        long id = 0;
+        if constexpr (MODE == PROJ_EMIT) id = a.id_base + (a.row_map ? a.row_map[row] : row);
+        for (int j = lane; j < a.D; j += 32) {
+          const float v = w[padj(j)];
           const int col = r * a.D + j;
           if constexpr (MODE == PROJ_ROWS) {
             a.out[row * (long)C + col] = v;
@@ -91,8 +89,7 @@ __global__ void __launch_bounds__(256) k_project(ProjArgs a) {
             if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v;
           } else {  // PROJ_EMIT
             if (a.col_active && !a.col_active[col]) continue;
-            const uint2 th = reinterpret_cast<const uint2*>(a.th)[col];
-            const long id = a.id_base + (a.row_map ? a.row_map[row] : row);
+            const uint2 th = __ldg(reinterpret_cast<const uint2*>(a.th) + col);
             if (fkey(v) >= th.x) {
               const unsigned pos = atomicAdd(&a.cnt[2 * col], 1u);
               if (pos < (unsigned)a.cap) a.cand[((long)2 * col) * a.cap + pos] = pack_key(v, (int)id);

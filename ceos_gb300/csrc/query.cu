@@ -108,6 +108,24 @@ CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, Ro
 CEOS_DEV int slot_id(uint64_t w) { return (int)(uint32_t)(w & 0xffffffffu); }
 CEOS_DEV float slot_val(uint64_t w) { return __uint_as_float((uint32_t)(w >> 32)); }
 
+// Shared-memory table accesses with explicit .shared instructions (a table
+// pointer carried through lambdas is otherwise treated as generic, and
+// generic-address atomics on shared memory are far slower).
+CEOS_DEV unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+CEOS_DEV int ld_volatile_shared(unsigned a) {
+  int v;
+  asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(v) : "r"(a));
+  return v;
+}
+CEOS_DEV int cas_shared(unsigned a, int cmp, int val) {
+  int old;
+  asm volatile("atom.shared.cas.b32 %0, [%1], %2, %3;" : "=r"(old) : "r"(a), "r"(cmp), "r"(val) : "memory");
+  return old;
+}
+CEOS_DEV void red_add_shared(unsigned a, float v) {
+  asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
 // Find or insert `id`; returns the slot index. Open addressing with double
 // hashing over a prime capacity (so every probe sequence visits every slot):
 // at the load factors a shared-memory table runs at, probe lengths have a
@@ -115,23 +133,46 @@ CEOS_DEV float slot_val(uint64_t w) { return __uint_as_float((uint32_t)(w >> 32)
 // because every probed column ends at a barrier that waits for the longest
 // insertion. The capacity exceeds the number of insertions, so a free slot
 // always exists; the sequence is still bounded and returns -1 if it ran out.
+template <bool SMEM>
 CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
   const uint32_t h1 = (uint32_t)id * 0x9E3779B1u;
   const uint32_t h2 = ((uint32_t)id ^ 0x5bd1e995u) * 0x85EBCA6Bu;
   int s = (int)(((uint64_t)h1 * (uint32_t)cap) >> 32);
   const int step = 1 + (int)(((uint64_t)h2 * (uint32_t)(cap - 1)) >> 32);
   int* keys = reinterpret_cast<int*>(t);
+  const unsigned base = SMEM ? smem_u32(t) : 0u;
   for (int probe = 0; probe < cap; ++probe) {
-    const int cur = *reinterpret_cast<volatile int*>(&keys[2 * s]);
+    int cur;
+    if (SMEM)
+      cur = ld_volatile_shared(base + 8u * (unsigned)s);
+    else
+      cur = *reinterpret_cast<volatile int*>(&keys[2 * s]);
     if (cur == id) return s;
     if (cur == -1) {
-      const int prev = atomicCAS(&keys[2 * s], -1, id);
+      const int prev = SMEM ? cas_shared(base + 8u * (unsigned)s, -1, id)
+                            : atomicCAS(&keys[2 * s], -1, id);
       if (prev == -1 || prev == id) return s;
     }
     s += step;
     if (s >= cap) s -= cap;
   }
   return -1;
+}
+
+// Add v to the value of slot `sl`. Within one probed column every id is
+// distinct when `distinct` holds, so no other thread touches the slot during
+// the column and a plain read-modify-write is exact; otherwise (streamCEOs,
+// whose stale rows may repeat an id) the add is atomic.
+template <bool SMEM>
+CEOS_DEV void table_add(uint64_t* t, int sl, float v, bool distinct) {
+  float* val = reinterpret_cast<float*>(&t[sl]) + 1;
+  if (distinct) {
+    *reinterpret_cast<volatile float*>(val) = *reinterpret_cast<volatile float*>(val) + v;
+  } else if (SMEM) {
+    red_add_shared(smem_u32(t) + 8u * (unsigned)sl + 4u, v);
+  } else {
+    atomicAdd(val, v);
+  }
 }
 
 struct QLayout {
@@ -217,9 +258,9 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
     // ---- 2. ordered accumulation / union of the probed bucket prefixes ----
     auto insert = [&](int id, float v) {
       if ((unsigned long)(unsigned)id >= npts) return;  // stale streamCEOs row
-      const int sl = table_slot(table, cap, id);
+      const int sl = table_slot<SMEM_TABLE>(table, cap, id);
       if (sl < 0) return;
-      if (MODE == Q_ESTIMATE) atomicAdd(reinterpret_cast<float*>(&table[sl]) + 1, v);
+      if (MODE == Q_ESTIMATE) table_add<SMEM_TABLE>(table, sl, v, a.distinct_ids != 0);
     };
     if (a.p <= kEPT * (int)blockDim.x) {
       int pid[kPrefetch][kEPT];
