@@ -33,7 +33,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-CFG = dict(n=1_000_000, d=128, nq=10_000, D=256, R=8, m=500, s=40, c=2000, k=10, seed=42)
+# Index and data of the plain-FP32 at-scale configuration. The metric asks for
+# queries/s at recall@10 >= 0.9: on this data the configured probe budget
+# (n_probed_vectors=40, n_cand=2000) reaches recall@10 = 0.64, so the headline
+# is taken at the smallest budget measured to clear 0.9 (s=120, c=8000,
+# recall 0.916); the configured point is reported beside it.
+CFG = dict(n=1_000_000, d=128, nq=10_000, D=256, R=8, m=500, s=120, c=8000, k=10, seed=42)
+CONFIG_POINT = dict(s=40, c=2000)
 WORKLOAD = "coCEOs-Est FP32 build+search, SIFT-shaped 1Mx128, 10k queries"
 
 
@@ -217,10 +223,10 @@ def run_reference(args, X, Q):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=15)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--ref-queries", type=int, default=64)
+    ap.add_argument("--ref-queries", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--recall-queries", type=int, default=200)
     args = ap.parse_args()
@@ -293,6 +299,18 @@ def main():
     rt.d2h(hi, dI)
     assert np.array_equal(hi, ids), "device-resident and host-call results differ"
 
+    # the configured probe budget (recall below the metric's floor)
+    idx.n_probed_vectors, idx.n_cand = CONFIG_POINT["s"], CONFIG_POINT["c"]
+    cp_ms = []
+    for i in range(args.warmup + args.steps):
+        _capi.check(L.ceos_flush_l2(flush))
+        t = dev_step()
+        if i >= args.warmup:
+            cp_ms.append(sum(t.values()))
+    cp_ids, _ = idx.search_coCEOs_Est(Q[:args.recall_queries], k)
+    idx.n_probed_vectors, idx.n_cand = CFG["s"], CFG["c"]
+
+
     # roofline of the dominant kernel (query estimate + rerank)
     s, p, c, m, C_ = CFG["s"], CFG["m"], CFG["c"], CFG["m"], CFG["D"] * CFG["R"]
     bytes_per_query = s * p * 8 + c * d * 4 + C_ * 4 + d * 4 + k * 8
@@ -310,13 +328,15 @@ def main():
     rq = args.recall_queries
     gt, _ = O.bruteforce(X, Q[:rq], 10, 0)
     rec = float(np.mean([len(np.intersect1d(a, b)) / 10 for a, b in zip(ids[:rq], gt)]))
+    cp_rec = float(np.mean([len(np.intersect1d(a, b)) / 10 for a, b in zip(cp_ids[:rq], gt)]))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        qps, cpu_build_s, _ = cpu_baseline_run(X, Q, 64, threads)
+        qps, cpu_build_s, _ = cpu_baseline_run(X, Q, 48, threads)
         cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-               "sample": "64 queries searched on the full 1Mx128 index built by the oracle",
+               "sample": "48 queries (same probe budget) searched on the full 1Mx128 index "
+                         "built by the oracle",
                "build_s": cpu_build_s}
 
     if rank == 0:
@@ -329,6 +349,9 @@ def main():
             "config": {"workload": WORKLOAD, **CFG, "l2": "flushed (512 MiB write) before every step",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "recall@10": rec, "recall_queries": rq,
+            "at_configured_budget": {"n_probed_vectors": CONFIG_POINT["s"], "n_cand": CONFIG_POINT["c"],
+                                     "value": ws * nq * len(cp_ms) / (sum(cp_ms) / 1e3),
+                                     "unit": "queries/s", "recall@10": cp_rec},
             "build_s": build_s, "build_phases_ms": build_phases,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,

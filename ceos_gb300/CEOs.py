@@ -255,6 +255,18 @@ class streamCEOs(_QueryAttrs):
     def set_threads(self, n_threads):
         _capi.check(self._L.ceos_stream_set_threads(self._h, int(n_threads)))
 
+    @property
+    def precision(self) -> str:
+        return getattr(self, "_precision", "fp32")
+
+    @precision.setter
+    def precision(self, v: str):
+        code = {"fp32": _capi.PRECISION_FP32, "split_bf16": _capi.PRECISION_SPLIT_BF16}.get(v)
+        if code is None:
+            raise ValueError("precision must be 'fp32' or 'split_bf16'")
+        _capi.check(self._L.ceos_stream_set_precision(self._h, code))
+        self._precision = v
+
     def clear(self):
         _capi.check(self._L.ceos_stream_clear(self._h))
 

@@ -71,6 +71,7 @@ SIGNATURES = {
     "ceos_stream_destroy": (None, [VP]),
     "ceos_stream_set_index_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "ceos_stream_set_threads": (C.c_int, [VP, C.c_int]),
+    "ceos_stream_set_precision": (C.c_int, [VP, C.c_int]),
     "ceos_stream_clear": (C.c_int, [VP]),
     "ceos_stream_set_query_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
     "ceos_stream_get_query_param": (C.c_int, [VP, IP, IP, IP]),

@@ -194,6 +194,8 @@ struct Core {
   int built = B_NONE;
   long n_rows = 0, head = 0, cap_rows = 0;
   DevBuf dX, dSigns, dP, dBids, dBvals;
+  DevBuf dXb;  // bfloat16 copy of the rows (split precision), same ring layout
+  bool xb_valid = false;
   DevBuf wStage, wQ, wQproj, wIds, wD, wTable, wProbes, wEst, wNewP, wNewX;
   Timer timer;
 
@@ -207,7 +209,9 @@ struct Core {
     seed = sd;
     fht = (D >= 1 && n_features >= 1) ? fht_dim(D, n_features) : 0;
     L = fht > 0 ? ilog2(fht) : 0;
-    ldx = (n_features + 3) & ~3;
+    // rows padded to a multiple of 8 floats: 16-byte aligned float4 chunks of
+    // the FP32 rows and 16-byte chunks of the bfloat16 copy
+    ldx = (n_features + 7) & ~7;
   }
 
   int ensure_device() {
@@ -234,8 +238,9 @@ struct Core {
   }
 
   void release_all() {
-    DevBuf* bufs[] = {&dX, &dSigns, &dP, &dBids, &dBvals, &wStage, &wQ, &wQproj, &wIds,
+    DevBuf* bufs[] = {&dX, &dSigns, &dP, &dBids, &dBvals, &dXb, &wStage, &wQ, &wQproj, &wIds,
                       &wD, &wTable, &wProbes, &wEst, &wNewP, &wNewX};
+    xb_valid = false;
     for (DevBuf* b : bufs) b->release();
     built = B_NONE;
     n_rows = head = cap_rows = 0;
@@ -403,6 +408,16 @@ struct Core {
 
   int fallback_columns = 0;
 
+  // Bfloat16 copy of the whole row ring for the split-precision scan, made
+  // on the first split search after a build and kept current by updates.
+  int ensure_bf16() {
+    if (precision != CEOS_PRECISION_SPLIT_BF16 || xb_valid) return CEOS_OK;
+    CUDA_TRY(dXb.ensure((size_t)cap_rows * ldx * 2));
+    CUDA_TRY(launch_to_bf16(dX.as<float>(), cap_rows * (long)ldx, dXb.as<uint16_t>(), stream));
+    xb_valid = true;
+    return CEOS_OK;
+  }
+
   // Stage queries (host or device, n x n_features) into wQ (n x ldx) and
   // project them into wQproj (n x C).
   int stage_queries(const float* Q, long nq, bool on_device) {
@@ -453,12 +468,17 @@ struct Core {
     q.bvals = dBvals.as<float>();
     q.P = dP.as<float>();
     q.distinct_ids = built == B_STREAM ? 0 : 1;
+    if (precision == CEOS_PRECISION_SPLIT_BF16) {
+      q.Xb = dXb.as<uint16_t>();
+      q.rescore = 4 * k;
+    }
     return q;
   }
 
   // coCEOs-Est / CEOs-Hash / stream searches over the buckets.
   int search_buckets(int mode, const float* Q, long nq, int k, int32_t* ids, float* dists,
                      bool on_device, cudaStream_t user_stream) {
+    ST_TRY(ensure_bf16());
     timer.begin(stream);
     ST_TRY(stage_queries(Q, nq, on_device));
     QueryArgs q = query_base(nq, k);
@@ -505,6 +525,7 @@ struct Core {
   }
 
   int search_dense(const float* Q, long nq, int k, int32_t* ids, float* dists, bool on_device) {
+    ST_TRY(ensure_bf16());
     timer.begin(stream);
     ST_TRY(stage_queries(Q, nq, on_device));
     QueryArgs q = query_base(nq, k);
@@ -905,6 +926,14 @@ int ceos_stream_set_index_param(ceos_stream* h, int n_proj, int n_repeats, int t
   return CEOS_OK;
 }
 
+int ceos_stream_set_precision(ceos_stream* h, int precision) {
+  if (!h) return fail(CEOS_ERR_ARG, "null handle");
+  if (precision != CEOS_PRECISION_FP32 && precision != CEOS_PRECISION_SPLIT_BF16)
+    return fail(CEOS_ERR_ARG, "unknown precision %d", precision);
+  h->core.precision = precision;
+  return CEOS_OK;
+}
+
 int ceos_stream_set_threads(ceos_stream* h, int n_threads) {
   if (!h) return fail(CEOS_ERR_ARG, "null handle");
   h->core.n_threads = n_threads;
@@ -1016,6 +1045,8 @@ int ceos_stream_update(ceos_stream* h, const float* Xn, int b, int n_del) {
     nx.release();
     c.cap_rows = ncap;
     c.head = 0;
+    c.dXb.release();
+    c.xb_valid = false;
   }
   if (b > 0) {
     const size_t rowb = (size_t)c.ldx * 4;
@@ -1026,6 +1057,13 @@ int ceos_stream_update(ceos_stream* h, const float* Xn, int b, int n_del) {
     if (b > first)
       CUDA_TRY(cudaMemcpyAsync(c.dX.p, c.wNewX.as<float>() + first * c.ldx, (b - first) * rowb,
                                cudaMemcpyDeviceToDevice, c.stream));
+    if (c.xb_valid) {  // keep the bfloat16 copy of the ring current
+      CUDA_TRY(launch_to_bf16(c.dX.as<float>() + pos * c.ldx, first * (long)c.ldx,
+                              c.dXb.as<uint16_t>() + pos * c.ldx, c.stream));
+      if (b > first)
+        CUDA_TRY(launch_to_bf16(c.dX.as<float>(), (b - first) * (long)c.ldx, c.dXb.as<uint16_t>(),
+                                c.stream));
+    }
   }
   c.head = (c.head + n_del) % c.cap_rows;
   c.n_rows = cur + b - n_del;

@@ -57,6 +57,10 @@ struct QueryArgs {
   const int* bids = nullptr;    // [C][2][m]
   const float* bvals = nullptr; // [C][2][m]
   const float* P = nullptr;     // dense CEOs-Est projections [C][n]
+  // split precision: bfloat16 copy of the rows (same ring layout, stride ldx)
+  // and the number of scan winners rescored in FP32 (0 = plain FP32 rerank)
+  const uint16_t* Xb = nullptr;
+  int rescore = 0;
   int* out_ids = nullptr;
   float* out_d = nullptr;
   // 1 when every bucket column holds distinct ids (CEOs / coCEOs indexes); a
@@ -89,5 +93,7 @@ cudaError_t launch_stream_merge(int C, int m, const float* newP, long b, long cu
 
 // ---- misc ----
 cudaError_t launch_pad_rows(const float* src, long n, int d, float* dst, int ldx, cudaStream_t st);
+// bfloat16 copy (round to nearest even) of n rows of stride ldx
+cudaError_t launch_to_bf16(const float* src, long n_elems, uint16_t* dst, cudaStream_t st);
 
 }  // namespace ceos

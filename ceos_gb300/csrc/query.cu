@@ -41,6 +41,12 @@ CEOS_DEV const float* row_ptr(const QueryArgs& a, int id) {
   return a.X + r * (long)a.ldx;
 }
 
+CEOS_DEV const uint16_t* row_ptr_bf16(const QueryArgs& a, int id) {
+  long r = a.head + id;
+  if (r >= a.cap_rows) r -= a.cap_rows;
+  return a.Xb + r * (long)a.ldx;
+}
+
 // Inner product of a query with one row, in the library's canonical order:
 // the row is split into float4 chunks; lane g (0..7) of an 8-lane group
 // accumulates chunks g, g+8, g+16, ... as a sequential FMA chain
@@ -85,6 +91,52 @@ CEOS_DEV float dot_g8(const float* __restrict__ q, const float* __restrict__ x, 
   return s;
 }
 
+// Approximate score for the split-precision scan: like dot_g8 but over
+// 8-element chunks of the bfloat16 row (16 bytes per lane per load); chunk c
+// goes to lane c mod 8, each lane a sequential FMA chain, then the butterfly.
+CEOS_DEV float dot_g8_bf16(const float* __restrict__ q, const uint16_t* __restrict__ x, int n8,
+                           int g, bool active) {
+  const uint4* x8 = reinterpret_cast<const uint4*>(x);
+  const float4* q4 = reinterpret_cast<const float4*>(q);
+  float s = 0.0f;
+  if (active) {
+    for (int c = g; c < n8; c += 8) {
+      const uint4 w = __ldcg(x8 + c);
+      const float4 qa = q4[2 * c], qb = q4[2 * c + 1];
+      s = __fmaf_rn(qa.x, __uint_as_float(w.x << 16), s);
+      s = __fmaf_rn(qa.y, __uint_as_float(w.x & 0xffff0000u), s);
+      s = __fmaf_rn(qa.z, __uint_as_float(w.y << 16), s);
+      s = __fmaf_rn(qa.w, __uint_as_float(w.y & 0xffff0000u), s);
+      s = __fmaf_rn(qb.x, __uint_as_float(w.z << 16), s);
+      s = __fmaf_rn(qb.y, __uint_as_float(w.z & 0xffff0000u), s);
+      s = __fmaf_rn(qb.z, __uint_as_float(w.w << 16), s);
+      s = __fmaf_rn(qb.w, __uint_as_float(w.w & 0xffff0000u), s);
+    }
+  }
+  s = s + __shfl_xor_sync(0xffffffffu, s, 4);
+  s = s + __shfl_xor_sync(0xffffffffu, s, 2);
+  s = s + __shfl_xor_sync(0xffffffffu, s, 1);
+  return s;
+}
+
+// Split-precision rerank of keys[0..n) in place (approximate bfloat16 scores).
+template <typename RowPtr>
+CEOS_DEV void rerank_bf16_inplace(uint64_t* keys, int n, const float* qv, int ldx, RowPtr row) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane & 7;
+  const int grp = lane >> 3;
+  const int warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  const int n8 = ldx >> 3;
+  for (int base = warp * 4; base < n; base += nw * 4) {
+    const int i = base + grp;
+    const bool active = i < n;
+    const int id = active ? key_id(keys[i]) : 0;
+    const float d = dot_g8_bf16(qv, active ? row(id) : nullptr, n8, g, active);
+    if (active && g == 0) keys[i] = pack_key(d, id);
+  }
+}
+
 // Rerank keys[0..n) in place: each holds a candidate id (packed key); it is
 // replaced by pack_key(<q, x_id>, id). Each warp scores four rows at a time,
 // one per 8-lane group.
@@ -103,6 +155,36 @@ CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, Ro
     const float d = dot_g8(qv, active ? row(id) : qv, n4, g, active);
     if (active && g == 0) keys[i] = pack_key(d, id);
   }
+}
+
+// Final scoring of a candidate list (keys hold candidate ids): exact FP32
+// rerank, or (split precision) the bfloat16 scan followed by an exact rescore
+// of the scan's best `a.rescore`, staged in `resc`. Returns the number of
+// leading keys that hold exact scores: n, or min(n, a.rescore) after the
+// rescored keys are copied to the front.
+CEOS_DEV int score_candidates(const QueryArgs& a, uint64_t* keys, int n, const float* qv,
+                              uint64_t* resc, uint32_t* hist, uint64_t* maybe, int maybe_cap,
+                              uint32_t* scratch) {
+  if (a.Xb == nullptr || a.rescore <= 0) {
+    rerank_inplace(keys, n, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
+    __syncthreads();
+    return n;
+  }
+  rerank_bf16_inplace(keys, n, qv, a.ldx, [&](int id) { return row_ptr_bf16(a, id); });
+  __syncthreads();
+  const int nr = block_topk_hist(
+      [&](long i, float& v, int& id) {
+        const uint64_t k = keys[i];
+        v = key_val(k);
+        id = key_id(k);
+        return true;
+      },
+      (long)n, a.rescore, resc, hist, maybe, maybe_cap, scratch);
+  rerank_inplace(resc, nr, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) keys[i] = resc[i];
+  __syncthreads();
+  return nr;
 }
 
 CEOS_DEV int slot_id(uint64_t w) { return (int)(uint32_t)(w & 0xffffffffu); }
@@ -176,7 +258,7 @@ CEOS_DEV void table_add(uint64_t* t, int sl, float v, bool distinct) {
 }
 
 struct QLayout {
-  size_t qv, pkeys, probes, topk, cand, hist, maybe, table, total;
+  size_t qv, pkeys, probes, topk, resc, cand, hist, maybe, table, total;
 };
 
 constexpr int kMaybe = 1024;  // threshold-bin buffer of the histogram top-K
@@ -200,6 +282,8 @@ __host__ __device__ inline QLayout q_layout(const QueryArgs& a, int mode) {
   o = al16(o + (size_t)(a.s > 0 ? a.s : 1) * 4);
   L.topk = o;
   o = al16(o + (size_t)np2(a.k > 0 ? a.k : 1) * 8);
+  L.resc = o;
+  o = al16(o + (size_t)(a.rescore > 0 ? a.rescore : 0) * 8);
   L.cand = o;
   if (mode == Q_ESTIMATE) o = al16(o + (size_t)(a.c > 0 ? a.c : 1) * 8);
   L.hist = o;
@@ -226,6 +310,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
   uint64_t* pkeys = reinterpret_cast<uint64_t*>(sm + Lq.pkeys);
   int* probes = reinterpret_cast<int*>(sm + Lq.probes);
   uint64_t* topk = reinterpret_cast<uint64_t*>(sm + Lq.topk);
+  uint64_t* resc = reinterpret_cast<uint64_t*>(sm + Lq.resc);
   uint64_t* cand = reinterpret_cast<uint64_t*>(sm + Lq.cand);
   uint32_t* hist = reinterpret_cast<uint32_t*>(sm + Lq.hist);
   uint64_t* maybe = reinterpret_cast<uint64_t*>(sm + Lq.maybe);
@@ -318,9 +403,8 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
             return id >= 0;
           },
           (long)cap, a.c, cand, hist, maybe, kMaybe, scratch);
-      // ---- 4. exact rerank, in place ----
-      rerank_inplace(cand, nc, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
-      __syncthreads();
+      // ---- 4. rerank (exact, or bfloat16 scan + exact rescore), in place ----
+      const int ns2 = score_candidates(a, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
       nres = block_topk_hist_sorted(
           [&](long i, float& v, int& id) {
             const uint64_t k = cand[i];
@@ -328,9 +412,44 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
             id = key_id(k);
             return true;
           },
-          (long)nc, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+          (long)ns2, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
     } else {
       // ---- union rerank in place over the table slots ----
+      if (a.Xb != nullptr && a.rescore > 0) {
+        // split precision: bfloat16 scan over the slots, exact rescore of the best
+        const int lane = threadIdx.x & 31;
+        const int g = lane & 7;
+        const int grp = lane >> 3;
+        const int warp = threadIdx.x >> 5;
+        const int nw = blockDim.x >> 5;
+        for (int base = warp * 4; base < cap; base += nw * 4) {
+          const int i = base + grp;
+          const uint64_t w = i < cap ? (uint64_t)(*reinterpret_cast<volatile uint64_t*>(&table[i])) : (uint64_t)kEmptySlot;
+          const int id = slot_id(w);
+          const bool active = id >= 0;
+          const float d = dot_g8_bf16(qv, active ? row_ptr_bf16(a, id) : nullptr, a.ldx >> 3, g, active);
+          __syncwarp();
+          if (i < cap && g == 0) table[i] = active ? pack_key(d, id) : 0ull;
+        }
+        __syncthreads();
+        const int nr = block_topk_hist(
+            [&](long i, float& v, int& id) {
+              const uint64_t k = *reinterpret_cast<volatile uint64_t*>(&table[i]);
+              v = key_val(k);
+              id = key_id(k);
+              return k != 0ull;
+            },
+            (long)cap, a.rescore, resc, hist, maybe, kMaybe, scratch);
+        rerank_inplace(resc, nr, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
+        __syncthreads();
+        nres = block_topk_hist_sorted(
+            [&](long i, float& v, int& id) {
+              v = key_val(resc[i]);
+              id = key_id(resc[i]);
+              return true;
+            },
+            (long)nr, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+      } else {
       {
         const int lane = threadIdx.x & 31;
         const int g = lane & 7;
@@ -356,6 +475,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
             return k != 0ull;
           },
           (long)cap, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+      }
     }
     for (int i = threadIdx.x; i < a.k; i += blockDim.x) {
       a.out_ids[(long)q * a.k + i] = i < nres ? key_id(topk[i]) : 0;
@@ -483,7 +603,8 @@ __global__ void __launch_bounds__(kQueryThreads) k_dense_select_rerank(QueryArgs
   const int k_cap = np2(a.k > 0 ? a.k : 1);
   float* qv = reinterpret_cast<float*>(sm);
   uint64_t* topk = reinterpret_cast<uint64_t*>(sm + al16((size_t)a.ldx * 4));
-  uint64_t* cand = topk + k_cap;
+  uint64_t* resc = topk + k_cap;
+  uint64_t* cand = resc + (a.rescore > 0 ? a.rescore : 0);
   uint32_t* hist = reinterpret_cast<uint32_t*>(cand + (a.c > 0 ? a.c : 1));
   uint64_t* maybe = reinterpret_cast<uint64_t*>(hist + kHistBins);
   for (int j = threadIdx.x; j < a.ldx; j += blockDim.x) qv[j] = a.Q[(long)q * a.ldx + j];
@@ -495,15 +616,14 @@ __global__ void __launch_bounds__(kQueryThreads) k_dense_select_rerank(QueryArgs
         return true;
       },
       a.n_points, a.c, cand, hist, maybe, kMaybe, scratch);
-  rerank_inplace(cand, nc, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
-  __syncthreads();
+  const int ns2 = score_candidates(a, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
   const int nres = block_topk_hist_sorted(
       [&](long i, float& v, int& id) {
         v = key_val(cand[i]);
         id = key_id(cand[i]);
         return true;
       },
-      (long)nc, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+      (long)ns2, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
   for (int i = threadIdx.x; i < a.k; i += blockDim.x) {
     a.out_ids[(long)q * a.k + i] = i < nres ? key_id(topk[i]) : 0;
     a.out_d[(long)q * a.k + i] = i < nres ? key_val(topk[i]) : 0.0f;
@@ -513,7 +633,8 @@ __global__ void __launch_bounds__(kQueryThreads) k_dense_select_rerank(QueryArgs
 cudaError_t launch_dense_select_rerank(const QueryArgs& a, int q0, int nq_chunk, cudaStream_t st) {
   if (nq_chunk <= 0) return cudaSuccess;
   const int k_cap = np2(a.k > 0 ? a.k : 1);
-  const size_t smem = al16((size_t)a.ldx * 4) + (size_t)k_cap * 8 + (size_t)(a.c > 0 ? a.c : 1) * 8 +
+  const size_t smem = al16((size_t)a.ldx * 4) + (size_t)k_cap * 8 +
+                      (size_t)(a.rescore > 0 ? a.rescore : 0) * 8 + (size_t)(a.c > 0 ? a.c : 1) * 8 +
                       (size_t)kHistBins * 4 + (size_t)kMaybe * 8;
   cudaError_t e = cudaFuncSetAttribute(k_dense_select_rerank,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

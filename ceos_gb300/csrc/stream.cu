@@ -11,6 +11,8 @@
 //
 // GPU form: one CTA per (column, end); the survivors and the new points'
 // projections (column-major [C][b]) form one key stream for the block top-m.
+#include <cuda_bf16.h>
+
 #include "kernels.h"
 #include "common.cuh"
 
@@ -81,6 +83,20 @@ cudaError_t launch_pad_rows(const float* src, long n, int d, float* dst, int ldx
   long blocks = (n * ldx + 255) / 256;
   if (blocks > 4096) blocks = 4096;
   k_pad_rows<<<(unsigned)blocks, 256, 0, st>>>(src, n, d, dst, ldx);
+  return cudaGetLastError();
+}
+
+// bfloat16 rows for the split-precision scan (round to nearest, ties to even).
+__global__ void k_to_bf16(const float* src, long n, uint16_t* dst) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = __bfloat16_as_ushort(__float2bfloat16_rn(src[i]));
+}
+
+cudaError_t launch_to_bf16(const float* src, long n_elems, uint16_t* dst, cudaStream_t st) {
+  if (n_elems <= 0) return cudaSuccess;
+  long blocks = (n_elems + 255) / 256;
+  if (blocks > 8192) blocks = 8192;
+  k_to_bf16<<<(unsigned)blocks, 256, 0, st>>>(src, n_elems, dst);
   return cudaGetLastError();
 }
 

@@ -95,7 +95,9 @@ int ceos_get_query_param(const ceos_index* h, int* n_probed_vectors, int* n_prob
  * ceos_build_ceos_hash. */
 int ceos_set_centering(ceos_index* h, int centering);
 int ceos_get_centering(const ceos_index* h, int* centering);
-/* CEOS_PRECISION_* for the next search (no counterpart in the reference). */
+/* CEOS_PRECISION_* for the next search (no counterpart in the reference). The split form
+ * scans the candidates' rows in bfloat16 (a copy made on the first split search) and
+ * rescores the best 4 * n_neighbors of that scan exactly in FP32. */
 int ceos_set_precision(ceos_index* h, int precision);
 
 /* build(dataset): python/python_wrapper.cpp:39 -> CEOs::build_CEOs, src/CEOs.cpp:18-98.
@@ -169,6 +171,9 @@ void ceos_stream_destroy(ceos_stream* h);
 int ceos_stream_set_index_param(ceos_stream* h, int n_proj, int n_repeats, int top_points,
                                 int n_threads, int random_seed);
 int ceos_stream_set_threads(ceos_stream* h, int n_threads);
+/* CEOS_PRECISION_* for the next estimate_search / hash_search (no counterpart in the
+ * reference). */
+int ceos_stream_set_precision(ceos_stream* h, int precision);
 int ceos_stream_clear(ceos_stream* h);
 int ceos_stream_set_query_param(ceos_stream* h, int n_probed_vectors, int n_probed_points,
                                 int n_cand);

@@ -306,6 +306,65 @@ static void write_topk(MinQue& q, int k, int* ids, float* dists) {
 }
 
 // ----------------------------------------------------------------------------
+// Split precision (no reference counterpart): rows rounded to bfloat16
+// (round to nearest, ties to even) for an approximate scan; the best
+// `rescore` candidates of the scan are rescored exactly with dot_fma.
+static inline float bf16_round(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) {  // inf / nan: truncate (keep nan quiet)
+    u &= 0xffff0000u;
+    if ((x != x)) u |= 0x00400000u;
+  } else {
+    u += 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+  }
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+// Approximate score: 8 partial sums over 8-element chunks (chunk c goes to
+// partial c mod 8), each a sequential fused multiply-add chain of q_j and the
+// bfloat16-rounded x_j, combined by the same butterfly as dot_fma.
+static inline float dot_bf16(const float* q, const float* x, int d) {
+  const int n8 = (d + 7) / 8;
+  float p[8];
+  for (int g = 0; g < 8; ++g) {
+    float s = 0.0f;
+    for (int c = g; c < n8; c += 8)
+      for (int e = 0; e < 8; ++e) {
+        const int j = 8 * c + e;
+        if (j < d) s = std::fma(q[j], bf16_round(x[j]), s);
+      }
+    p[g] = s;
+  }
+  float t[8];
+  for (int g = 0; g < 8; ++g) t[g] = p[g] + p[g ^ 4];
+  for (int g = 0; g < 8; ++g) p[g] = t[g] + t[g ^ 2];
+  for (int g = 0; g < 8; ++g) t[g] = p[g] + p[g ^ 1];
+  return t[0];
+}
+
+// Rerank a candidate set: plain (exact scores for all), or split (bfloat16
+// scan of all, exact rescore of the best `rescore`). Returns the top-k heap.
+template <typename RowFn>
+static void rerank(const std::vector<int>& cand, const float* qv, int d, int k, int split,
+                   int rescore, RowFn row, MinQue& topk) {
+  if (!split) {
+    for (int id : cand) offer(topk, k, id, dot_fma(qv, row(id), d));
+    return;
+  }
+  MinQue approx;
+  for (int id : cand) offer(approx, rescore, id, dot_bf16(qv, row(id), d));
+  while (!approx.empty()) {
+    const int id = approx.top().id;
+    approx.pop();
+    offer(topk, k, id, dot_fma(qv, row(id), d));
+  }
+}
+
+// ----------------------------------------------------------------------------
 // CEOs index (src/CEOs.h:18-114).
 struct OracleCEOs {
   int n_points, n_features;
@@ -313,6 +372,7 @@ struct OracleCEOs {
   int n_threads = -1;
   int n_probed_vectors = 10, n_probed_points = 10, n_cand = 10;
   bool centering = false;
+  int split = 0, rescore_mult = 4;  // split precision: rescore rescore_mult * k
   int fhtDim = 0;
   std::vector<float> X;        // n x d
   std::vector<float> P;        // dense: n x C row-major
@@ -405,12 +465,14 @@ struct OracleCEOs {
         }
         MinQue cand;
         for (int i = 0; i < n_points; ++i) offer(cand, n_cand, i, est[i]);
-        MinQue topk;
+        std::vector<int> cids;
         while (!cand.empty()) {
-          int id = cand.top().id;
+          cids.push_back(cand.top().id);
           cand.pop();
-          offer(topk, k, id, dot_fma(qv, &X[(size_t)id * d], d));
         }
+        MinQue topk;
+        rerank(cids, qv, d, k, split, rescore_mult * k,
+               [&](int id) { return &X[(size_t)id * d]; }, topk);
         write_topk(topk, k, ids + (size_t)q * k, dists + (size_t)q * k);
       }
     }
@@ -448,12 +510,14 @@ struct OracleCEOs {
         }
         MinQue cand;
         for (auto& kv : est) offer(cand, n_cand, kv.first, kv.second);
-        MinQue topk;
+        std::vector<int> cids;
         while (!cand.empty()) {
-          int id = cand.top().id;
+          cids.push_back(cand.top().id);
           cand.pop();
-          offer(topk, k, id, dot_fma(qv, &X[(size_t)id * d], d));
         }
+        MinQue topk;
+        rerank(cids, qv, d, k, split, rescore_mult * k,
+               [&](int id) { return &X[(size_t)id * d]; }, topk);
         write_topk(topk, k, ids + (size_t)q * k, dists + (size_t)q * k);
       }
     }
@@ -484,9 +548,12 @@ struct OracleCEOs {
           size_t o = (size_t)c * 2 * m + (tag < 0 ? m : 0);
           for (int j = 0; j < p; ++j) seen[B_ids[o + j]] = 1;
         }
-        MinQue topk;
+        std::vector<int> cids;
         for (int i = 0; i < n_points; ++i)
-          if (seen[i]) offer(topk, k, i, dot_fma(qv, &X[(size_t)i * d], d));
+          if (seen[i]) cids.push_back(i);
+        MinQue topk;
+        rerank(cids, qv, d, k, split, rescore_mult * k,
+               [&](int id) { return &X[(size_t)id * d]; }, topk);
         write_topk(topk, k, ids + (size_t)q * k, dists + (size_t)q * k);
       }
     }
@@ -501,6 +568,7 @@ struct OracleStream {
   int n_proj = 256, n_rotate = 3, top_m = 100, n_repeats = 1, seed = -1;
   int n_threads = -1;
   int n_probed_vectors = 10, n_probed_points = 10, n_cand = 10;
+  int split = 0, rescore_mult = 4;
   int fhtDim = 0;
   std::deque<std::vector<float>> X;
   std::vector<int> B_ids;      // [C][2][m]
@@ -642,12 +710,13 @@ struct OracleStream {
         }
         MinQue cand;
         for (auto& kv : est) offer(cand, n_cand, kv.first, kv.second);
-        MinQue topk;
+        std::vector<int> cids;
         while (!cand.empty()) {
-          int id = cand.top().id;
+          cids.push_back(cand.top().id);
           cand.pop();
-          offer(topk, k, id, dot_fma(qv, X[id].data(), d));
         }
+        MinQue topk;
+        rerank(cids, qv, d, k, split, rescore_mult * k, [&](int id) { return X[id].data(); }, topk);
         write_topk(topk, k, ids + (size_t)q * k, dists + (size_t)q * k);
       }
     }
@@ -679,9 +748,11 @@ struct OracleStream {
             if (id >= 0 && id < n_points) seen[id] = 1;  // stale ids skipped, as above
           }
         }
-        MinQue topk;
+        std::vector<int> cids;
         for (int i = 0; i < n_points; ++i)
-          if (seen[i]) offer(topk, k, i, dot_fma(qv, X[i].data(), d));
+          if (seen[i]) cids.push_back(i);
+        MinQue topk;
+        rerank(cids, qv, d, k, split, rescore_mult * k, [&](int id) { return X[id].data(); }, topk);
         write_topk(topk, k, ids + (size_t)q * k, dists + (size_t)q * k);
       }
     }
@@ -779,6 +850,17 @@ void orc_ceos_get_query(void* h, int* s, int* p, int* c) {
   *c = o->n_cand;
 }
 int orc_ceos_fht_dim(void* h) { return ((OracleCEOs*)h)->fhtDim; }
+void orc_ceos_set_split(void* h, int split, int mult) {
+  ((OracleCEOs*)h)->split = split;
+  ((OracleCEOs*)h)->rescore_mult = mult;
+}
+void orc_stream_set_split(void* h, int split, int mult) {
+  ((OracleStream*)h)->split = split;
+  ((OracleStream*)h)->rescore_mult = mult;
+}
+float orc_bf16_round(float x) { return bf16_round(x); }
+float orc_dot_bf16(const float* q, const float* x, int d) { return dot_bf16(q, x, d); }
+float orc_dot(const float* q, const float* x, int d) { return dot_fma(q, x, d); }
 int orc_ceos_build_dense(void* h, const float* X) { return ((OracleCEOs*)h)->build_dense(X); }
 int orc_ceos_build_coceos(void* h, const float* X) { return ((OracleCEOs*)h)->build_buckets(X, true); }
 int orc_ceos_build_hash(void* h, const float* X) { return ((OracleCEOs*)h)->build_buckets(X, false); }

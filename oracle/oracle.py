@@ -87,6 +87,16 @@ def lib():
             L.orc_ceos_get_query.argtypes = [vp] + [C.POINTER(C.c_int)] * 3
             L.orc_ceos_get_query.restype = None
             L.orc_ceos_fht_dim.argtypes = [vp]
+            L.orc_ceos_set_split.argtypes = [vp, C.c_int, C.c_int]
+            L.orc_ceos_set_split.restype = None
+            L.orc_stream_set_split.argtypes = [vp, C.c_int, C.c_int]
+            L.orc_stream_set_split.restype = None
+            L.orc_bf16_round.argtypes = [C.c_float]
+            L.orc_bf16_round.restype = C.c_float
+            L.orc_dot_bf16.argtypes = [_F32P, _F32P, C.c_int]
+            L.orc_dot_bf16.restype = C.c_float
+            L.orc_dot.argtypes = [_F32P, _F32P, C.c_int]
+            L.orc_dot.restype = C.c_float
             for nm in ("dense", "coceos", "hash"):
                 getattr(L, f"orc_ceos_build_{nm}").argtypes = [vp, _F32P]
                 getattr(L, f"orc_ceos_search_{nm}").argtypes = [vp, _F32P, C.c_int, C.c_int, _I32P, _F32P]
@@ -169,6 +179,21 @@ def bruteforce(X, Q, k: int, n_threads: int = 0):
     sc = np.zeros((nq, k), np.float64)
     _check(lib().orc_bruteforce(X, X.shape[0], X.shape[1], Q, nq, k, ids, sc, n_threads))
     return ids, sc
+
+
+def bf16_round(x) -> np.ndarray:
+    x = _f32(x)
+    return np.array([lib().orc_bf16_round(float(v)) for v in x.ravel()], np.float32).reshape(x.shape)
+
+
+def dot(q, x) -> float:
+    q, x = _f32(q), _f32(x)
+    return float(lib().orc_dot(q, x, q.shape[0]))
+
+
+def dot_bf16(q, x) -> float:
+    q, x = _f32(q), _f32(x)
+    return float(lib().orc_dot_bf16(q, x, q.shape[0]))
 
 
 def ref_ffht(v) -> np.ndarray | None:
@@ -254,6 +279,15 @@ class CEOs(_Attrs):
     def set_threads(self, n_threads):
         pass
 
+    @property
+    def precision(self):
+        return getattr(self, "_precision", "fp32")
+
+    @precision.setter
+    def precision(self, v):
+        self._precision = v
+        self._L.orc_ceos_set_split(self._h, 1 if v == "split_bf16" else 0, 4)
+
     def _search(self, fn, Q, k):
         Q = _f32(Q)
         nq = Q.shape[0]
@@ -322,6 +356,15 @@ class streamCEOs(_Attrs):
     @property
     def size(self):
         return int(self._L.orc_stream_size(self._h))
+
+    @property
+    def precision(self):
+        return getattr(self, "_precision", "fp32")
+
+    @precision.setter
+    def precision(self, v):
+        self._precision = v
+        self._L.orc_stream_set_split(self._h, 1 if v == "split_bf16" else 0, 4)
 
     def build(self, dataset):
         X = _f32(dataset)

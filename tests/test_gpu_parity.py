@@ -3,7 +3,8 @@
 Bit-exact expectations (same tie rule on both sides):
   * projections (sign flips + FWHT, src/CEOs.cpp:58-88) - every bit;
   * bucket ids and values (src/CEOs.cpp:377-428);
-  * search ids and scores (both compute the score as a sequential FMA chain).
+  * search ids and scores (both compute each score in the same fixed order:
+    8 strided FMA chains over float4 chunks, then a butterfly).
 Estimates are accumulated in the reference's probe pop order on both sides,
 so candidate sets match exactly too.
 """
@@ -268,3 +269,64 @@ def test_recall_vs_fp64(gpu, oracle):
     g.n_probed_vectors, g.n_cand = 20, 500
     ids, dists = g.search_coCEOs_Est(Q, 10)
     assert recall(ids, gt) > 0.85
+
+
+@pytest.mark.parametrize("kind", ["coceos", "dense", "hash"])
+def test_split_bf16_exact(gpu, oracle, kind):
+    """Split precision: bfloat16 scan of the candidates, exact FP32 rescore of
+    the best 4k. Both sides round rows to bfloat16 the same way (nearest,
+    ties to even) and use the same scan order, so even the approximate scan
+    agrees and the final ids and scores are bit-exact."""
+    n, d = 3000, 150  # d not a multiple of 8: padded rows
+    X = gist_like(n, d, seed=101)
+    Q = gist_like(40, d, seed=102)
+    g, o = build_pair(gpu, oracle, X, 256, 2, 60, 42, kind=kind)
+    for idx in (g, o):
+        idx.n_probed_vectors, idx.n_cand = 24, 300
+        idx.precision = "split_bf16"
+    fn = {"coceos": "search_coCEOs_Est", "dense": "search", "hash": "search_CEOs_Hash"}[kind]
+    a = getattr(g, fn)(Q, 10)
+    b = getattr(o, fn)(Q, 10)
+    assert np.array_equal(a[0], b[0]) and bits_equal(a[1], b[1])
+    # switching back to FP32 gives the plain results again
+    for idx in (g, o):
+        idx.precision = "fp32"
+    a = getattr(g, fn)(Q, 10)
+    b = getattr(o, fn)(Q, 10)
+    assert np.array_equal(a[0], b[0]) and bits_equal(a[1], b[1])
+
+
+def test_stream_split_bf16_exact(gpu, oracle):
+    d = 40
+    X = gist_like(5000, d, seed=111)
+    Q = gist_like(24, d, seed=112)
+    g, o = gpu.streamCEOs(d), oracle.streamCEOs(d)
+    for s in (g, o):
+        s.setIndexParam(64, 2, 50, 2, 42)
+        s.build(X[:1000])
+        s.n_probed_vectors, s.n_probed_points, s.n_cand = 16, 50, 200
+        s.precision = "split_bf16"
+    for a, b, nd in [(1000, 1600, 300), (1600, 4000, 1000), (4000, 5000, 2500)]:
+        for s in (g, o):
+            s.update(X[a:b], nd)
+        ai, ad = g.estimate_search(Q, 10)
+        bi, bd = o.estimate_search(Q, 10)
+        assert np.array_equal(ai, bi) and bits_equal(ad, bd)
+        ai, ad = g.hash_search(Q, 10)
+        bi, bd = o.hash_search(Q, 10)
+        assert np.array_equal(ai, bi) and bits_equal(ad, bd)
+
+
+def test_split_bf16_recall_matches_fp32(gpu, oracle):
+    n, d = 20000, 256
+    X = gist_like(n, d, seed=121)
+    Q = gist_like(100, d, seed=122)
+    gt, _ = oracle.bruteforce(X, Q, 10)
+    g = gpu.CEOs(n, d)
+    g.setIndexParam(256, 4, 200, 1, 42)
+    g.build_coCEOs_Est(X)
+    g.n_probed_vectors, g.n_cand = 30, 1000
+    r32 = recall(g.search_coCEOs_Est(Q, 10)[0], gt)
+    g.precision = "split_bf16"
+    rsp = recall(g.search_coCEOs_Est(Q, 10)[0], gt)
+    assert abs(r32 - rsp) <= 0.01, (r32, rsp)

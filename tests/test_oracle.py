@@ -139,3 +139,14 @@ def test_oracle_stream_fifo(oracle):
     assert bids.min() >= 0 and bids.max() < 400
     with pytest.raises(ValueError):
         s.update(X[:1], 1000)
+
+
+def test_bf16_rounding_nearest_even(oracle):
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.standard_normal(5000).astype(np.float32) * 100,
+                        np.array([1.00390625, 1.005859375, -1.00390625, 0.0, -0.0, 65504.0,
+                                  3.3895314e38, 1e-40], np.float32)])
+    u = x.view(np.uint32).astype(np.uint64)
+    ref = (((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000) & 0xFFFFFFFF).astype(np.uint32).view(np.float32)
+    got = oracle.bf16_round(x)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
