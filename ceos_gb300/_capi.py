@@ -26,6 +26,8 @@ ERR_CUDA = -7
 ERR_NO_DEVICE = -8
 ERR_UNSUPPORTED = -9
 ERR_DEVICE_LIMIT = -10
+ERR_TIMEOUT = -11
+ERR_BUSY = -12
 
 ALGO_DENSE, ALGO_COCEOS, ALGO_HASH = 0, 1, 2
 PRECISION_FP32, PRECISION_SPLIT_BF16 = 0, 1
@@ -35,6 +37,25 @@ I32P = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 U8P = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 VP = C.c_void_p
 IP = C.POINTER(C.c_int)
+U64P = C.POINTER(C.c_uint64)
+
+
+class ServerConfig(C.Structure):
+    """struct ceos_server_config."""
+    _fields_ = [("algo", C.c_int), ("n_slots", C.c_int), ("max_batch", C.c_int),
+                ("max_neighbors", C.c_int), ("max_probed_vectors", C.c_int),
+                ("mem_budget_bytes", C.c_longlong), ("use_graphs", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    """struct ceos_server_stats."""
+    _fields_ = [("requests", C.c_longlong), ("queries", C.c_longlong), ("batches", C.c_longlong),
+                ("graph_launches", C.c_longlong), ("graphs_captured", C.c_longlong),
+                ("updates", C.c_longlong), ("slots", C.c_int), ("slot_bytes", C.c_longlong),
+                ("mean_batch_queries", C.c_double), ("p50_ms", C.c_double), ("p90_ms", C.c_double),
+                ("p99_ms", C.c_double), ("max_ms", C.c_double), ("mean_ms", C.c_double),
+                ("busy_s", C.c_double)]
+
 
 # name -> (restype, argtypes); every entry point declared in include/ceos_gb300.h
 SIGNATURES = {
@@ -81,6 +102,15 @@ SIGNATURES = {
     "ceos_stream_hash_search": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
     "ceos_stream_size": (C.c_int, [VP, IP]),
     "ceos_stream_get_buckets": (C.c_int, [VP, I32P, F32P]),
+    "ceos_server_config_init": (C.c_int, [C.POINTER(ServerConfig)]),
+    "ceos_server_create": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),
+    "ceos_server_create_stream": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),
+    "ceos_server_destroy": (None, [VP]),
+    "ceos_server_submit": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, VP, VP, U64P]),
+    "ceos_server_submit_update": (C.c_int, [VP, VP, C.c_int, C.c_int, U64P]),
+    "ceos_server_wait": (C.c_int, [VP, C.c_uint64, C.c_int]),
+    "ceos_server_get_stats": (C.c_int, [VP, C.POINTER(ServerStats)]),
+    "ceos_server_reset_stats": (C.c_int, [VP]),
 }
 
 _lock = threading.Lock()
@@ -124,6 +154,8 @@ def check(status: int) -> None:
     if status in (ERR_ARG, ERR_PROBED_POINTS, ERR_PROBED_VECTORS, ERR_UPDATE_DEL, ERR_UPDATE_TOPM,
                   ERR_UNSUPPORTED):
         raise ValueError(msg)
-    if status == ERR_NOT_BUILT:
+    if status in (ERR_NOT_BUILT, ERR_BUSY):
         raise RuntimeError(msg)
+    if status == ERR_TIMEOUT:
+        raise TimeoutError(msg)
     raise CEOsError(f"[{status}] {msg}")

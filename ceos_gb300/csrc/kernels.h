@@ -61,8 +61,19 @@ struct QueryArgs {
   // and the number of scan winners rescored in FP32 (0 = plain FP32 rerank)
   const uint16_t* Xb = nullptr;
   int rescore = 0;
+  // with per-query k (q_k), query q rescores rescore_per_k * k_q (<= rescore)
+  int rescore_per_k = 0;
   int* out_ids = nullptr;
   float* out_d = nullptr;
+  // optional per-query parameters (serving batches that mix requests): probes
+  // s_q <= s, neighbours k_q <= k, and the offset of query q's k_q results in
+  // out_ids / out_d. Null = every query uses s and k at offset q * k.
+  const int* q_s = nullptr;
+  const int* q_k = nullptr;
+  const long* q_off = nullptr;
+  const int* q_cap = nullptr;  // per-query hash-table capacity (<= table_cap)
+  // optional device-side query count (graph replays of a fixed-capacity batch)
+  const int* d_nq = nullptr;
   // 1 when every bucket column holds distinct ids (CEOs / coCEOs indexes); a
   // streamCEOs index can keep stale rows that repeat an id within a column
   int distinct_ids = 0;

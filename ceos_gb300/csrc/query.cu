@@ -162,10 +162,10 @@ CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, Ro
 // of the scan's best `a.rescore`, staged in `resc`. Returns the number of
 // leading keys that hold exact scores: n, or min(n, a.rescore) after the
 // rescored keys are copied to the front.
-CEOS_DEV int score_candidates(const QueryArgs& a, uint64_t* keys, int n, const float* qv,
+CEOS_DEV int score_candidates(const QueryArgs& a, int rq, uint64_t* keys, int n, const float* qv,
                               uint64_t* resc, uint32_t* hist, uint64_t* maybe, int maybe_cap,
                               uint32_t* scratch) {
-  if (a.Xb == nullptr || a.rescore <= 0) {
+  if (a.Xb == nullptr || rq <= 0) {
     rerank_inplace(keys, n, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
     __syncthreads();
     return n;
@@ -179,7 +179,7 @@ CEOS_DEV int score_candidates(const QueryArgs& a, uint64_t* keys, int n, const f
         id = key_id(k);
         return true;
       },
-      (long)n, a.rescore, resc, hist, maybe, maybe_cap, scratch);
+      (long)n, rq, resc, hist, maybe, maybe_cap, scratch);
   rerank_inplace(resc, nr, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
   __syncthreads();
   for (int i = threadIdx.x; i < nr; i += blockDim.x) keys[i] = resc[i];
@@ -318,12 +318,19 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
   // shared-memory tables get shared (not generic) loads and atomics.
   uint64_t* table = SMEM_TABLE ? reinterpret_cast<uint64_t*>(sm + Lq.table)
                                : a.gtable + (long)blockIdx.x * a.table_cap;
-  const int cap = a.table_cap;
+  const int cap_max = a.table_cap;
   const int s_cap = np2(a.s > 0 ? a.s : 1);
   const int k_cap = np2(a.k > 0 ? a.k : 1);
   const unsigned long npts = (unsigned long)a.n_points;
 
-  for (int q = blockIdx.x; q < a.nq; q += gridDim.x) {
+  const int nq = a.d_nq ? min(*a.d_nq, a.nq) : a.nq;
+  for (int q = blockIdx.x; q < nq; q += gridDim.x) {
+    const int sq = a.q_s ? min(a.q_s[q], a.s) : a.s;
+    const int kq = a.q_k ? min(a.q_k[q], a.k) : a.k;
+    const long oq = a.q_off ? a.q_off[q] : (long)q * a.k;
+    // per-query table capacity (a prime sized for this query's probes)
+    const int cap = a.q_cap ? min(a.q_cap[q], cap_max) : cap_max;
+    const int rq = (a.q_k && a.rescore_per_k > 0) ? min(a.rescore, a.rescore_per_k * kq) : a.rescore;
     for (int j = threadIdx.x; j < a.ldx; j += blockDim.x) qv[j] = a.Q[(long)q * a.ldx + j];
     // ---- 1. probes: top-s |projection|, consumed worst first ----
     const float* qp = a.qproj + (long)q * a.C;
@@ -333,7 +340,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
           id = (int)i;
           return true;
         },
-        (long)a.C, a.s, pkeys, s_cap, hist, maybe, kMaybe, scratch);
+        (long)a.C, sq, pkeys, s_cap, hist, maybe, kMaybe, scratch);
     for (int j = threadIdx.x; j < ns; j += blockDim.x) {
       const int col = key_id(pkeys[ns - 1 - j]);
       probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
@@ -404,7 +411,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
           },
           (long)cap, a.c, cand, hist, maybe, kMaybe, scratch);
       // ---- 4. rerank (exact, or bfloat16 scan + exact rescore), in place ----
-      const int ns2 = score_candidates(a, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
+      const int ns2 = score_candidates(a, rq, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
       nres = block_topk_hist_sorted(
           [&](long i, float& v, int& id) {
             const uint64_t k = cand[i];
@@ -412,10 +419,10 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
             id = key_id(k);
             return true;
           },
-          (long)ns2, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+          (long)ns2, kq, topk, k_cap, hist, maybe, kMaybe, scratch);
     } else {
       // ---- union rerank in place over the table slots ----
-      if (a.Xb != nullptr && a.rescore > 0) {
+      if (a.Xb != nullptr && rq > 0) {
         // split precision: bfloat16 scan over the slots, exact rescore of the best
         const int lane = threadIdx.x & 31;
         const int g = lane & 7;
@@ -439,7 +446,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
               id = key_id(k);
               return k != 0ull;
             },
-            (long)cap, a.rescore, resc, hist, maybe, kMaybe, scratch);
+            (long)cap, rq, resc, hist, maybe, kMaybe, scratch);
         rerank_inplace(resc, nr, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
         __syncthreads();
         nres = block_topk_hist_sorted(
@@ -448,7 +455,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
               id = key_id(resc[i]);
               return true;
             },
-            (long)nr, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+            (long)nr, kq, topk, k_cap, hist, maybe, kMaybe, scratch);
       } else {
       {
         const int lane = threadIdx.x & 31;
@@ -474,12 +481,12 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
             id = key_id(k);
             return k != 0ull;
           },
-          (long)cap, a.k, topk, k_cap, hist, maybe, kMaybe, scratch);
+          (long)cap, kq, topk, k_cap, hist, maybe, kMaybe, scratch);
       }
     }
-    for (int i = threadIdx.x; i < a.k; i += blockDim.x) {
-      a.out_ids[(long)q * a.k + i] = i < nres ? key_id(topk[i]) : 0;
-      a.out_d[(long)q * a.k + i] = i < nres ? key_val(topk[i]) : 0.0f;
+    for (int i = threadIdx.x; i < kq; i += blockDim.x) {
+      a.out_ids[oq + i] = i < nres ? key_id(topk[i]) : 0;
+      a.out_d[oq + i] = i < nres ? key_val(topk[i]) : 0.0f;
     }
     __syncthreads();
   }
@@ -616,7 +623,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_dense_select_rerank(QueryArgs
         return true;
       },
       a.n_points, a.c, cand, hist, maybe, kMaybe, scratch);
-  const int ns2 = score_candidates(a, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
+  const int ns2 = score_candidates(a, a.rescore, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
   const int nres = block_topk_hist_sorted(
       [&](long i, float& v, int& id) {
         v = key_val(cand[i]);

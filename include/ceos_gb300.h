@@ -42,6 +42,8 @@ extern "C" {
 #define CEOS_ERR_NO_DEVICE (-8)       /* no CUDA device visible */
 #define CEOS_ERR_UNSUPPORTED (-9)     /* size outside what the kernels support */
 #define CEOS_ERR_DEVICE_LIMIT (-10)   /* a bounded device-side loop gave up */
+#define CEOS_ERR_TIMEOUT (-11)        /* ceos_server_wait: the request is still running */
+#define CEOS_ERR_BUSY (-12)           /* the index is owned by a server (ceos_server_create*) */
 
 /* Search algorithms for ceos_search_device. */
 #define CEOS_ALGO_DENSE 0   /* CEOs-Est:   build / search */
@@ -193,6 +195,79 @@ int ceos_stream_hash_search(ceos_stream* h, const float* Q, int n_queries, int n
 /* Current number of points (the reference's deque_X.size()). */
 int ceos_stream_size(const ceos_stream* h, int* n_points);
 int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals);
+
+/* ---- serving loop (no reference counterpart) ----------------------------
+ * The reference answers one blocking batch per call (python/python_wrapper.cpp:36-48,
+ * :62-71). A server keeps a built index resident on the device and answers requests
+ * submitted from any host thread. Each request is a block of queries with its own
+ * n_neighbors and n_probed_vectors (n_probed_points and n_cand are the index's, as
+ * set when the server is created), or, on a streamCEOs index, an update.
+ *
+ * One worker thread packs the queued query requests, in arrival order, into batches
+ * of at most max_batch queries on n_slots device slots; a request larger than the
+ * free room is split. A batch is launched as soon as a slot is free, so requests
+ * that arrive while other batches run are admitted into the next slot that frees
+ * up, and the slots' batches overlap on the device (continuous batching). Each slot
+ * holds fixed device memory (slot_bytes in the stats); slots are created only while
+ * they fit mem_budget_bytes. A batch (query upload, projection, the persistent query
+ * kernel, result download) is replayed as a CUDA graph captured per (slot,
+ * power-of-two batch size). An update waits until no batch is in flight, so every
+ * request sees the index as of its place in the queue.
+ *
+ * A request's results are the same, bit for bit, whatever it is batched with, and
+ * equal those of the index's own search with the same n_probed_vectors, n_neighbors
+ * and precision.
+ *
+ * While a server exists, the index's own build, update, search, clear and set_*
+ * calls return CEOS_ERR_BUSY. Destroy the server (it finishes queued work) before
+ * the index. */
+typedef struct ceos_server ceos_server;
+
+typedef struct ceos_server_config {
+  int algo;               /* CEOS_ALGO_COCEOS (coCEOs-Est; streamCEOs estimate_search) or
+                             CEOS_ALGO_HASH (CEOs-Hash; streamCEOs hash_search) */
+  int n_slots;            /* batches in flight, >= 1 */
+  int max_batch;          /* queries per batch, >= 1 */
+  int max_neighbors;      /* largest n_neighbors of a request */
+  int max_probed_vectors; /* largest n_probed_vectors of a request */
+  long long mem_budget_bytes; /* device bytes for the slots; 0 = no limit */
+  int use_graphs;         /* 1 = replay batches as CUDA graphs, 0 = launch them directly */
+} ceos_server_config;
+
+typedef struct ceos_server_stats {
+  long long requests;        /* query requests completed since the last reset */
+  long long queries;         /* queries launched */
+  long long batches;         /* batches launched */
+  long long graph_launches;  /* batches launched as graph replays */
+  long long graphs_captured; /* graphs captured (since creation) */
+  long long updates;         /* updates applied */
+  int slots;                 /* slots created under the memory budget */
+  long long slot_bytes;      /* device bytes of one slot */
+  double mean_batch_queries;
+  double p50_ms, p90_ms, p99_ms, max_ms, mean_ms; /* request latency: submit to results written */
+  double busy_s;             /* first submit to last completion since the last reset */
+} ceos_server_stats;
+
+/* Defaults: algo COCEOS, 4 slots, max_batch 256, max_neighbors 100,
+ * max_probed_vectors 80, no budget, graphs on. */
+int ceos_server_config_init(ceos_server_config* cfg);
+int ceos_server_create(ceos_index* h, const ceos_server_config* cfg, ceos_server** out);
+int ceos_server_create_stream(ceos_stream* h, const ceos_server_config* cfg, ceos_server** out);
+/* Finishes queued work, then frees the server. */
+void ceos_server_destroy(ceos_server* s);
+/* Queue n_queries x n_features queries (copied at the call). n_probed_vectors <= 0
+ * means the index's current value. ids / dists (n_queries x n_neighbors, best first)
+ * are written before the request completes and must stay valid until then. */
+int ceos_server_submit(ceos_server* s, const float* Q, int n_queries, int n_neighbors,
+                       int n_probed_vectors, int32_t* ids, float* dists, uint64_t* ticket);
+/* streamCEOs update (src/streamCEOs.cpp:174-369) in queue order; rows copied at the call. */
+int ceos_server_submit_update(ceos_server* s, const float* X_new, int n_new, int n_del,
+                              uint64_t* ticket);
+/* Block until the request completes (timeout_ms < 0: no limit); returns its status,
+ * CEOS_ERR_TIMEOUT if it is still running. A completed ticket is released. */
+int ceos_server_wait(ceos_server* s, uint64_t ticket, int timeout_ms);
+int ceos_server_get_stats(ceos_server* s, ceos_server_stats* out);
+int ceos_server_reset_stats(ceos_server* s);
 
 #ifdef __cplusplus
 }

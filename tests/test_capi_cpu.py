@@ -85,3 +85,18 @@ def test_no_cpu_fallback(ceos):
     idx.setIndexParam(16, 1, 4, 1, 0)
     with pytest.raises(_capi.CEOsError, match="no CUDA device"):
         idx.build_coCEOs_Est(np.ones((64, 8), np.float32))
+
+
+def test_server_rejects_unbuilt_index(ceos):
+    from ceos_gb300 import _capi
+    from ceos_gb300.serving import Server
+
+    cfg = _capi.ServerConfig()
+    assert _capi.lib().ceos_server_config_init(cfg) == 0
+    assert (cfg.algo, cfg.n_slots, cfg.max_batch, cfg.max_neighbors, cfg.max_probed_vectors,
+            cfg.mem_budget_bytes, cfg.use_graphs) == (_capi.ALGO_COCEOS, 4, 256, 100, 80, 0, 1)
+    idx = ceos.CEOs(100, 8)
+    with pytest.raises(RuntimeError, match="built"):
+        Server(idx)
+    with pytest.raises(ValueError):
+        Server(idx, algo="dense")
