@@ -55,6 +55,117 @@ def sift_like(n, d, seed):
     return out
 
 
+# Served-queries configuration: ImageNet-shaped 2.34M x 150 index, open-loop
+# Poisson request stream.
+SERVE = dict(n=2_340_000, d=150, D=256, R=16, m=1000, p=1000, c=1000, seed=42,
+             rate=2000.0, stream_seed=7, requests=4000, ks=(1, 10, 100), ss=(10, 20, 40, 80),
+             n_slots=4, max_batch=256)
+
+
+def imagenet_like(n, d, seed):
+    """Rows N(0, I_d) scaled by LogNormal(0, 0.7)."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, d), np.float32)
+    step = 250_000
+    for i in range(0, n, step):
+        j = min(n, i + step)
+        out[i:j] = rng.standard_normal((j - i, d), dtype=np.float32)
+        out[i:j] *= rng.lognormal(0.0, 0.7, (j - i, 1)).astype(np.float32)
+    return out
+
+
+def request_stream(cfg, pool):
+    """Open-loop Poisson arrivals (rate cfg['rate'] requests/s, seed
+    cfg['stream_seed']); each request is clip(round(LogNormal(2.5, 1.0)), 1, 256)
+    queries taken from `pool`, with k and n_probed_vectors drawn uniformly from
+    cfg['ks'] and cfg['ss']."""
+    rng = np.random.default_rng(cfg["stream_seed"])
+    n = cfg["requests"]
+    t = np.cumsum(rng.exponential(1.0 / cfg["rate"], n))
+    sizes = np.clip(np.round(rng.lognormal(2.5, 1.0, n)), 1, 256).astype(int)
+    ks = rng.choice(cfg["ks"], n)
+    ss = rng.choice(cfg["ss"], n)
+    offs = rng.integers(0, len(pool) - 256, n)
+    return [(float(t[i]), pool[offs[i]:offs[i] + sizes[i]], int(ks[i]), int(ss[i]))
+            for i in range(n)]
+
+
+def run_served(idx, reqs, precision, open_loop=True):
+    """Drive the serving loop with `reqs`; returns (stats, results)."""
+    from ceos_gb300.serving import Server
+
+    idx.precision = precision
+    srv = Server(idx, algo="coceos", n_slots=SERVE["n_slots"], max_batch=SERVE["max_batch"],
+                 max_neighbors=max(SERVE["ks"]), max_probed_vectors=max(SERVE["ss"]))
+    # warm up: capture every batch-size graph of every slot
+    warm = [srv.submit(reqs[i][1], reqs[i][2], reqs[i][3]) for i in range(min(64, len(reqs)))]
+    for r in warm:
+        srv.wait(r)
+    srv.reset_stats()
+    out = []
+    t0 = time.perf_counter()
+    for t_arr, Qr, k, s in reqs:
+        if open_loop:
+            while time.perf_counter() - t0 < t_arr:
+                pass
+        out.append(srv.submit(Qr, k, s))
+    res = [srv.wait(r) for r in out]
+    st = srv.stats()
+    srv.close()
+    return st, res
+
+
+def served_leg(args):
+    """Served queries (config of the request loop): build the 2.34M x 150 index,
+    drive the open-loop stream through the server in FP32 and split-BF16, and at
+    saturation (all requests queued at once); recall@k per request against the
+    GPU FP64 ground truth on a sample of requests."""
+    import ceos_gb300.CEOs as CEOs
+    from ceos_gb300 import _capi
+
+    cfg = SERVE
+    X = imagenet_like(cfg["n"], cfg["d"], 11)
+    pool = imagenet_like(50_000, cfg["d"], 12)
+    idx = CEOs.CEOs(cfg["n"], cfg["d"])
+    idx.setIndexParam(cfg["D"], cfg["R"], cfg["m"], -1, cfg["seed"])
+    t0 = time.perf_counter()
+    idx.build_coCEOs_Est(X)
+    build_s = time.perf_counter() - t0
+    idx.n_probed_points, idx.n_cand = cfg["p"], cfg["c"]
+    reqs = request_stream(cfg, pool)
+    out = {"config": {k: v for k, v in cfg.items()}, "build_s": build_s,
+           "build_phases_ms": idx.last_timings()}
+    sample = reqs[:100]
+    nsq = sum(len(r[1]) for r in sample)
+    gtQ = np.concatenate([r[1] for r in sample])
+    gt_ids, _ = _capi.bruteforce_fp64(X, gtQ, max(cfg["ks"]))
+    for prec in ("fp32", "split_bf16"):
+        st, res = run_served(idx, reqs, prec, open_loop=True)
+        sat, _ = run_served(idx, reqs, prec, open_loop=False)
+        # recall@min(k, 10) of the sampled requests, by n_probed_vectors
+        rec = {}
+        row = 0
+        for (t_arr, Qr, k, s), (ids, _) in zip(sample, res[:len(sample)]):
+            kk = min(k, 10)
+            g = gt_ids[row:row + len(Qr), :kk]
+            row += len(Qr)
+            rec.setdefault(s, []).extend(len(np.intersect1d(a[:kk], b)) / kk for a, b in zip(ids, g))
+        out[prec] = {
+            "open_loop": {"offered_req_per_s": cfg["rate"], "queries": st["queries"],
+                          "requests": st["requests"], "wall_s": st["busy_s"],
+                          "queries_per_s": st["queries"] / st["busy_s"],
+                          "p50_ms": st["p50_ms"], "p90_ms": st["p90_ms"], "p99_ms": st["p99_ms"],
+                          "max_ms": st["max_ms"], "mean_batch_queries": st["mean_batch_queries"],
+                          "graph_launches": st["graph_launches"]},
+            "saturation": {"queries_per_s": sat["queries"] / sat["busy_s"], "p50_ms": sat["p50_ms"],
+                           "p99_ms": sat["p99_ms"], "mean_batch_queries": sat["mean_batch_queries"]},
+            "recall_at_min_k_10_by_probes": {str(s): float(np.mean(v)) for s, v in sorted(rec.items())},
+            "recall_queries": nsq,
+        }
+    idx.precision = "fp32"
+    return out
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -229,8 +340,17 @@ def main():
     ap.add_argument("--ref-queries", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--recall-queries", type=int, default=200)
+    ap.add_argument("--only", choices=["served"], default=None,
+                    help="run one secondary leg alone and print its JSON")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     os.environ.setdefault("CEOS_GB300_LOG", "0")
+    if args.only == "served":
+        from ceos_gb300 import _capi
+
+        _capi.lib().ceos_set_log_level(0)
+        print(json.dumps({"served": served_leg(args)}))
+        return 0
 
     X = sift_like(CFG["n"], CFG["d"], 7)
     Q = sift_like(CFG["nq"], CFG["d"], 8)

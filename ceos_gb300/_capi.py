@@ -102,6 +102,8 @@ SIGNATURES = {
     "ceos_stream_hash_search": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
     "ceos_stream_size": (C.c_int, [VP, IP]),
     "ceos_stream_get_buckets": (C.c_int, [VP, I32P, F32P]),
+    "ceos_bruteforce_fp64": (C.c_int, [F32P, C.c_long, C.c_int, F32P, C.c_int, C.c_int, I32P,
+                                       np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")]),
     "ceos_server_config_init": (C.c_int, [C.POINTER(ServerConfig)]),
     "ceos_server_create": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),
     "ceos_server_create_stream": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),
@@ -159,3 +161,13 @@ def check(status: int) -> None:
     if status == ERR_TIMEOUT:
         raise TimeoutError(msg)
     raise CEOsError(f"[{status}] {msg}")
+
+
+def bruteforce_fp64(X, Q, k: int):
+    """Exact FP64 top-k inner products on the GPU (ground truth for recall)."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Q = np.ascontiguousarray(Q, dtype=np.float32)
+    ids = np.zeros((Q.shape[0], k), np.int32)
+    scores = np.zeros((Q.shape[0], k), np.float64)
+    check(lib().ceos_bruteforce_fp64(X, X.shape[0], X.shape[1], Q, Q.shape[0], k, ids, scores))
+    return ids, scores

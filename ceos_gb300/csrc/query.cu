@@ -15,23 +15,22 @@
 //     are accumulated in.
 //  2. estimate: for each probed column in that order, its first p bucket
 //     entries are accumulated into an open-addressing hash table keyed by
-//     point id (in shared memory when it fits, else in a per-CTA L2-resident
-//     workspace). Within one column the ids are distinct, so each table
-//     value receives its terms in exactly the reference's order; a barrier
-//     separates columns. Values start at -0.0, so the first addition
-//     reproduces the reference's "assign on first sight".
-//  3. top-c candidates by estimate (block radix select on packed keys).
-//  4. exact rerank: one thread per candidate computes the inner product as a
-//     sequential FMA chain over the row, then the block selects the top-k,
-//     written best first with zero fill past the number of results
-//     (src/CEOs.cpp:659-666).
+//     point id (keys and values in two arrays; in shared memory when it fits,
+//     else in a per-CTA L2-resident workspace). Within one column the ids are
+//     distinct, so each table value receives its terms in exactly the
+//     reference's order; a barrier separates columns. A value starts as its
+//     first term (the reference's "assign on first sight").
+//  3. top-c candidates by estimate (block histogram select on packed keys).
+//  4. exact rerank: groups of 8 lanes compute one inner product each (lane g
+//     accumulates the float4 chunks g, g+8, ... with FMA, then a butterfly
+//     over the 8 lanes), then the block selects the top-k, written best first
+//     with zero fill past the number of results (src/CEOs.cpp:659-666).
 #include "kernels.h"
 #include "common.cuh"
 
 namespace ceos {
 
 constexpr int kQueryThreads = 512;
-constexpr uint64_t kEmptySlot = (0x80000000ull << 32) | 0xffffffffull;  // id -1, value -0.0
 
 CEOS_DEV float abs_ref(float v) { return v < 0 ? -v : v; }
 
@@ -187,8 +186,6 @@ CEOS_DEV int score_candidates(const QueryArgs& a, int rq, uint64_t* keys, int n,
   return nr;
 }
 
-CEOS_DEV int slot_id(uint64_t w) { return (int)(uint32_t)(w & 0xffffffffu); }
-CEOS_DEV float slot_val(uint64_t w) { return __uint_as_float((uint32_t)(w >> 32)); }
 
 // Shared-memory table accesses with explicit .shared instructions (a table
 // pointer carried through lambdas is otherwise treated as generic, and
@@ -215,25 +212,32 @@ CEOS_DEV void red_add_shared(unsigned a, float v) {
 // because every probed column ends at a barrier that waits for the longest
 // insertion. The capacity exceeds the number of insertions, so a free slot
 // always exists; the sequence is still bounded and returns -1 if it ran out.
+//
+// The table is two arrays, keys[cap] (int32 ids, -1 = empty) and vals[cap]
+// (float sums), so that the random key probes spread over all 32 shared-memory
+// banks. `fresh` reports that this call inserted the id.
 template <bool SMEM>
-CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
+CEOS_DEV int table_slot(int* keys, int cap, int id, bool& fresh) {
   const uint32_t h1 = (uint32_t)id * 0x9E3779B1u;
   const uint32_t h2 = ((uint32_t)id ^ 0x5bd1e995u) * 0x85EBCA6Bu;
   int s = (int)(((uint64_t)h1 * (uint32_t)cap) >> 32);
   const int step = 1 + (int)(((uint64_t)h2 * (uint32_t)(cap - 1)) >> 32);
-  int* keys = reinterpret_cast<int*>(t);
-  const unsigned base = SMEM ? smem_u32(t) : 0u;
+  const unsigned base = SMEM ? smem_u32(keys) : 0u;
+  fresh = false;
   for (int probe = 0; probe < cap; ++probe) {
     int cur;
     if (SMEM)
-      cur = ld_volatile_shared(base + 8u * (unsigned)s);
+      cur = ld_volatile_shared(base + 4u * (unsigned)s);
     else
-      cur = *reinterpret_cast<volatile int*>(&keys[2 * s]);
+      cur = *reinterpret_cast<volatile int*>(&keys[s]);
     if (cur == id) return s;
     if (cur == -1) {
-      const int prev = SMEM ? cas_shared(base + 8u * (unsigned)s, -1, id)
-                            : atomicCAS(&keys[2 * s], -1, id);
-      if (prev == -1 || prev == id) return s;
+      const int prev = SMEM ? cas_shared(base + 4u * (unsigned)s, -1, id) : atomicCAS(&keys[s], -1, id);
+      if (prev == -1) {
+        fresh = true;
+        return s;
+      }
+      if (prev == id) return s;
     }
     s += step;
     if (s >= cap) s -= cap;
@@ -243,15 +247,17 @@ CEOS_DEV int table_slot(uint64_t* t, int cap, int id) {
 
 // Add v to the value of slot `sl`. Within one probed column every id is
 // distinct when `distinct` holds, so no other thread touches the slot during
-// the column and a plain read-modify-write is exact; otherwise (streamCEOs,
-// whose stale rows may repeat an id) the add is atomic.
+// the column and a plain read-modify-write is exact; a fresh slot takes v
+// itself (its sum starts at the additive identity -0.0f, and -0.0f + v == v),
+// stored without reading. Otherwise (streamCEOs, whose stale rows may repeat
+// an id) the add is atomic on a value initialised to -0.0f.
 template <bool SMEM>
-CEOS_DEV void table_add(uint64_t* t, int sl, float v, bool distinct) {
-  float* val = reinterpret_cast<float*>(&t[sl]) + 1;
+CEOS_DEV void table_add(float* vals, int sl, float v, bool distinct, bool fresh) {
+  float* val = vals + sl;
   if (distinct) {
-    *reinterpret_cast<volatile float*>(val) = *reinterpret_cast<volatile float*>(val) + v;
+    *reinterpret_cast<volatile float*>(val) = fresh ? v : *reinterpret_cast<volatile float*>(val) + v;
   } else if (SMEM) {
-    red_add_shared(smem_u32(t) + 8u * (unsigned)sl + 4u, v);
+    red_add_shared(smem_u32(val), v);
   } else {
     atomicAdd(val, v);
   }
@@ -301,8 +307,11 @@ size_t query_buckets_smem(const QueryArgs& a, int mode) { return q_layout(a, mod
 constexpr int kPrefetch = 4;  // bucket columns in flight
 constexpr int kEPT = 2;       // bucket entries per thread per column on the prefetch path
 
-template <int MODE, bool SMEM_TABLE>
-__global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
+// MINB = CTAs per SM the register budget is sized for: 1 (128 registers per
+// thread) when a shared-memory table leaves room for one CTA, 2 (64 registers)
+// when two CTAs fit, so that the latency-bound accumulation has 32 warps per SM.
+template <int MODE, bool SMEM_TABLE, int MINB>
+__global__ void __launch_bounds__(kQueryThreads, MINB) k_query_buckets(QueryArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint32_t scratch[16];
   const QLayout Lq = q_layout(a, MODE);
@@ -316,9 +325,10 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
   uint64_t* maybe = reinterpret_cast<uint64_t*>(sm + Lq.maybe);
   // The table pointer's address space is fixed per instantiation so that
   // shared-memory tables get shared (not generic) loads and atomics.
-  uint64_t* table = SMEM_TABLE ? reinterpret_cast<uint64_t*>(sm + Lq.table)
-                               : a.gtable + (long)blockIdx.x * a.table_cap;
   const int cap_max = a.table_cap;
+  int* tkeys = SMEM_TABLE ? reinterpret_cast<int*>(sm + Lq.table)
+                          : reinterpret_cast<int*>(a.gtable + (long)blockIdx.x * cap_max);
+  float* tvals = reinterpret_cast<float*>(tkeys + cap_max);
   const int s_cap = np2(a.s > 0 ? a.s : 1);
   const int k_cap = np2(a.k > 0 ? a.k : 1);
   const unsigned long npts = (unsigned long)a.n_points;
@@ -345,14 +355,18 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
       const int col = key_id(pkeys[ns - 1 - j]);
       probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
     }
-    for (int i = threadIdx.x; i < cap; i += blockDim.x) table[i] = kEmptySlot;
+    for (int i = threadIdx.x; i < cap; i += blockDim.x) {
+      tkeys[i] = -1;
+      if (!a.distinct_ids) tvals[i] = -0.0f;
+    }
     __syncthreads();
     // ---- 2. ordered accumulation / union of the probed bucket prefixes ----
     auto insert = [&](int id, float v) {
       if ((unsigned long)(unsigned)id >= npts) return;  // stale streamCEOs row
-      const int sl = table_slot<SMEM_TABLE>(table, cap, id);
+      bool fresh;
+      const int sl = table_slot<SMEM_TABLE>(tkeys, cap, id, fresh);
       if (sl < 0) return;
-      if (MODE == Q_ESTIMATE) table_add<SMEM_TABLE>(table, sl, v, a.distinct_ids != 0);
+      if (MODE == Q_ESTIMATE) table_add<SMEM_TABLE>(tvals, sl, v, a.distinct_ids != 0, fresh);
     };
     if (a.p <= kEPT * (int)blockDim.x) {
       int pid[kPrefetch][kEPT];
@@ -404,9 +418,8 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
       // ---- 3. top-c candidates by estimate ----
       const int nc = block_topk_hist(
           [&](long i, float& v, int& id) {
-            const uint64_t w = *reinterpret_cast<volatile uint64_t*>(&table[i]);
-            id = slot_id(w);
-            v = slot_val(w);
+            id = reinterpret_cast<volatile int*>(tkeys)[i];
+            v = reinterpret_cast<volatile float*>(tvals)[i];
             return id >= 0;
           },
           (long)cap, a.c, cand, hist, maybe, kMaybe, scratch);
@@ -431,20 +444,17 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
         const int nw = blockDim.x >> 5;
         for (int base = warp * 4; base < cap; base += nw * 4) {
           const int i = base + grp;
-          const uint64_t w = i < cap ? (uint64_t)(*reinterpret_cast<volatile uint64_t*>(&table[i])) : (uint64_t)kEmptySlot;
-          const int id = slot_id(w);
+          const int id = i < cap ? reinterpret_cast<volatile int*>(tkeys)[i] : -1;
           const bool active = id >= 0;
           const float d = dot_g8_bf16(qv, active ? row_ptr_bf16(a, id) : nullptr, a.ldx >> 3, g, active);
-          __syncwarp();
-          if (i < cap && g == 0) table[i] = active ? pack_key(d, id) : 0ull;
+          if (active && g == 0) tvals[i] = d;
         }
         __syncthreads();
         const int nr = block_topk_hist(
             [&](long i, float& v, int& id) {
-              const uint64_t k = *reinterpret_cast<volatile uint64_t*>(&table[i]);
-              v = key_val(k);
-              id = key_id(k);
-              return k != 0ull;
+              id = reinterpret_cast<volatile int*>(tkeys)[i];
+              v = reinterpret_cast<volatile float*>(tvals)[i];
+              return id >= 0;
             },
             (long)cap, rq, resc, hist, maybe, kMaybe, scratch);
         rerank_inplace(resc, nr, qv, a.ldx, [&](int id) { return row_ptr(a, id); });
@@ -465,21 +475,18 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
         const int nw = blockDim.x >> 5;
         for (int base = warp * 4; base < cap; base += nw * 4) {
           const int i = base + grp;
-          const uint64_t w = i < cap ? (uint64_t)(*reinterpret_cast<volatile uint64_t*>(&table[i])) : (uint64_t)kEmptySlot;
-          const int id = slot_id(w);
+          const int id = i < cap ? reinterpret_cast<volatile int*>(tkeys)[i] : -1;
           const bool active = id >= 0;
           const float d = dot_g8(qv, active ? row_ptr(a, id) : qv, a.ldx >> 2, g, active);
-          __syncwarp();
-          if (i < cap && g == 0) table[i] = active ? pack_key(d, id) : 0ull;
+          if (active && g == 0) tvals[i] = d;
         }
       }
       __syncthreads();
       nres = block_topk_hist_sorted(
           [&](long i, float& v, int& id) {
-            const uint64_t k = *reinterpret_cast<volatile uint64_t*>(&table[i]);
-            v = key_val(k);
-            id = key_id(k);
-            return k != 0ull;
+            id = reinterpret_cast<volatile int*>(tkeys)[i];
+            v = reinterpret_cast<volatile float*>(tvals)[i];
+            return id >= 0;
           },
           (long)cap, kq, topk, k_cap, hist, maybe, kMaybe, scratch);
       }
@@ -492,33 +499,48 @@ __global__ void __launch_bounds__(kQueryThreads) k_query_buckets(QueryArgs a) {
   }
 }
 
-template <int MODE, bool SM>
+template <int MODE, bool SM, int MINB>
 static cudaError_t launch_qb(const QueryArgs& a, int grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_query_buckets<MODE, SM>,
+  cudaError_t e = cudaFuncSetAttribute(k_query_buckets<MODE, SM, MINB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_query_buckets<MODE, SM><<<grid, kQueryThreads, smem, st>>>(a);
+  k_query_buckets<MODE, SM, MINB><<<grid, kQueryThreads, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+// Two CTAs per SM when their shared memory fits (the 64-register variant).
+static bool two_per_sm(size_t smem) {
+  int dev = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return 2 * (smem + 1024) <= (size_t)per_sm;
+}
+
+template <int MODE>
+static cudaError_t launch_mode(const QueryArgs& a, int grid, size_t smem, cudaStream_t st) {
+  if (!a.table_in_smem) return launch_qb<MODE, false, 2>(a, grid, smem, st);
+  return two_per_sm(smem) ? launch_qb<MODE, true, 2>(a, grid, smem, st)
+                          : launch_qb<MODE, true, 1>(a, grid, smem, st);
 }
 
 cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem,
                                  cudaStream_t st) {
   if (a.nq <= 0) return cudaSuccess;
-  if (mode == Q_ESTIMATE)
-    return a.table_in_smem ? launch_qb<Q_ESTIMATE, true>(a, grid, smem, st)
-                           : launch_qb<Q_ESTIMATE, false>(a, grid, smem, st);
-  return a.table_in_smem ? launch_qb<Q_UNION, true>(a, grid, smem, st)
-                         : launch_qb<Q_UNION, false>(a, grid, smem, st);
+  return mode == Q_ESTIMATE ? launch_mode<Q_ESTIMATE>(a, grid, smem, st)
+                            : launch_mode<Q_UNION>(a, grid, smem, st);
 }
 
-template <int MODE, bool SM>
+template <int MODE, bool SM, int MINB>
 static int occ_qb(size_t smem) {
   int n = 0;
-  cudaError_t e = cudaFuncSetAttribute(k_query_buckets<MODE, SM>,
+  cudaError_t e = cudaFuncSetAttribute(k_query_buckets<MODE, SM, MINB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_buckets<MODE, SM>, kQueryThreads,
-                                                      smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_buckets<MODE, SM, MINB>,
+                                                      kQueryThreads, smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -526,9 +548,15 @@ static int occ_qb(size_t smem) {
   return n;
 }
 
+template <int MODE>
+static int occ_mode(size_t smem, bool table_in_smem) {
+  if (!table_in_smem) return occ_qb<MODE, false, 2>(smem);
+  return two_per_sm(smem) ? occ_qb<MODE, true, 2>(smem) : occ_qb<MODE, true, 1>(smem);
+}
+
 int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem) {
-  if (mode == Q_ESTIMATE) return table_in_smem ? occ_qb<Q_ESTIMATE, true>(smem) : occ_qb<Q_ESTIMATE, false>(smem);
-  return table_in_smem ? occ_qb<Q_UNION, true>(smem) : occ_qb<Q_UNION, false>(smem);
+  return mode == Q_ESTIMATE ? occ_mode<Q_ESTIMATE>(smem, table_in_smem)
+                            : occ_mode<Q_UNION>(smem, table_in_smem);
 }
 
 // ---------------------------------------------------------------------------

@@ -196,6 +196,15 @@ int ceos_stream_hash_search(ceos_stream* h, const float* Q, int n_queries, int n
 int ceos_stream_size(const ceos_stream* h, int* n_points);
 int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals);
 
+/* ---- ground truth (no reference counterpart in the library) -------------
+ * Exact top-k maximum inner products of Q (nq x d) against X (n x d), row-major host
+ * float32, computed on the GPU in FP64 (float products are exact in double; double
+ * sums); ids and FP64 scores best first, ties towards the smaller id. Replaces the
+ * faiss IndexFlatIP ground truth of the reference's scripts (test/utils.py:35-55),
+ * for recall = |exact ∩ approx| / k (test/utils.py:27-32). k <= 1024. */
+int ceos_bruteforce_fp64(const float* X, long n, int d, const float* Q, int nq, int k,
+                         int32_t* ids, double* scores);
+
 /* ---- serving loop (no reference counterpart) ----------------------------
  * The reference answers one blocking batch per call (python/python_wrapper.cpp:36-48,
  * :62-71). A server keeps a built index resident on the device and answers requests

@@ -330,3 +330,20 @@ def test_split_bf16_recall_matches_fp32(gpu, oracle):
     g.precision = "split_bf16"
     rsp = recall(g.search_coCEOs_Est(Q, 10)[0], gt)
     assert abs(r32 - rsp) <= 0.01, (r32, rsp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,d,k,kind", [(50000, 100, 10, "netflix"), (20000, 16, 100, "sift"),
+                                        (1000, 33, 1, "netflix"), (50, 7, 100, "sift")])
+def test_bruteforce_fp64_matches_oracle(gpu, oracle, n, d, k, kind):
+    """The GPU FP64 ground truth equals the oracle's sequential double sums bit for
+    bit (float products are exact in double and both add in feature order), ties
+    (integer data) broken towards the smaller id, zero-filled past n."""
+    from ceos_gb300 import _capi
+
+    X = netflix_like(n, d, seed=n) if kind == "netflix" else sift_like(n, d, seed=n)
+    Q = gaussian_queries(70, d, seed=3) if kind == "netflix" else sift_like(70, d, seed=4)
+    gi, gs = _capi.bruteforce_fp64(X, Q, k)
+    oi, os_ = oracle.bruteforce(X, Q, k)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gs.view(np.uint64), os_.view(np.uint64))
