@@ -290,6 +290,25 @@ class streamCEOs(_QueryAttrs):
         ptr = X.ctypes.data if X.shape[0] else None
         _capi.check(self._L.ceos_stream_update(self._h, C.c_void_p(ptr), X.shape[0], int(n_delPoints)))
 
+    def set_reserve(self, reserve: int):
+        """Exact maintenance (no reference counterpart): with reserve >= 0, set before
+        build, each column end keeps top_points + reserve entries and every bucket is
+        the exact top-m over the live points after each update and delete; -1 keeps
+        the reference's maintenance (src/streamCEOs.cpp:262-358)."""
+        _capi.check(self._L.ceos_stream_set_reserve(self._h, int(reserve)))
+
+    @property
+    def reserve(self) -> int:
+        r = C.c_int()
+        _capi.check(self._L.ceos_stream_get_reserve(self._h, C.byref(r)))
+        return r.value
+
+    def delete(self, ids):
+        """Delete points by current id (0 .. size-1); later ids move down, as
+        erasing from the reference's deque would. Needs set_reserve before build."""
+        a = np.ascontiguousarray(np.asarray(ids, dtype=np.int32).ravel())
+        _capi.check(self._L.ceos_stream_delete(self._h, a.ctypes.data if a.size else None, a.size))
+
     def _search(self, fn, queries, n_neighbors, verbose):
         Q = _rows(queries, self.n_features, "queries")
         k = int(n_neighbors)

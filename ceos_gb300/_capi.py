@@ -102,6 +102,9 @@ SIGNATURES = {
     "ceos_stream_hash_search": (C.c_int, [VP, F32P, C.c_int, C.c_int, C.c_int, I32P, F32P]),
     "ceos_stream_size": (C.c_int, [VP, IP]),
     "ceos_stream_get_buckets": (C.c_int, [VP, I32P, F32P]),
+    "ceos_stream_set_reserve": (C.c_int, [VP, C.c_int]),
+    "ceos_stream_get_reserve": (C.c_int, [VP, IP]),
+    "ceos_stream_delete": (C.c_int, [VP, VP, C.c_int]),
     "ceos_bruteforce_fp64": (C.c_int, [F32P, C.c_long, C.c_int, F32P, C.c_int, C.c_int, I32P,
                                        np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")]),
     "ceos_server_config_init": (C.c_int, [C.POINTER(ServerConfig)]),
@@ -110,6 +113,7 @@ SIGNATURES = {
     "ceos_server_destroy": (None, [VP]),
     "ceos_server_submit": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, VP, VP, U64P]),
     "ceos_server_submit_update": (C.c_int, [VP, VP, C.c_int, C.c_int, U64P]),
+    "ceos_server_submit_delete": (C.c_int, [VP, VP, C.c_int, U64P]),
     "ceos_server_wait": (C.c_int, [VP, C.c_uint64, C.c_int]),
     "ceos_server_get_stats": (C.c_int, [VP, C.POINTER(ServerStats)]),
     "ceos_server_reset_stats": (C.c_int, [VP]),

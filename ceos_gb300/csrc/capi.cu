@@ -415,6 +415,14 @@ int ceos_stream_build(ceos_stream* h, const float* X, int n_points) {
     c.release_all();
     return st;
   }
+  if (c.reserve >= 0) {
+    std::vector<int> cnt((size_t)c.C() * 2, c.stride());
+    CUDA_TRY(c.dCnt.ensure(cnt.size() * 4));
+    CUDA_TRY(cudaMemcpyAsync(c.dCnt.p, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, c.stream));
+    CUDA_TRY(c.dTau.ensure(cnt.size() * sizeof(uint2)));
+    CUDA_TRY(launch_init_tau(c.C(), c.stride(), c.n_rows, c.dBids.as<int>(), c.dBvals.as<float>(),
+                             c.dTau.as<uint2>(), c.stream));
+  }
   CUDA_TRY(cudaStreamSynchronize(c.stream));
   c.timer.finish();
   c.built = B_STREAM;
@@ -460,8 +468,16 @@ int ceos_host::stream_update(ceos_stream* h, const float* Xn, int b, int n_del) 
     CUDA_TRY(launch_project(a, PROJ_COLS, c.L, c.sms, c.stream));
   }
   c.timer.mark("project");
-  CUDA_TRY(launch_stream_merge(Cc, c.top_m, c.wNewP.as<float>(), b, cur, n_del, c.dBids.as<int>(),
-                               c.dBvals.as<float>(), c.stream));
+  DevBuf flags;
+  if (c.reserve >= 0) {
+    CUDA_TRY(flags.ensure((size_t)Cc * 2 * 4));
+    CUDA_TRY(launch_stream_merge_exact(Cc, c.stride(), c.top_m, c.wNewP.as<float>(), b, cur, n_del,
+                                       c.dBids.as<int>(), c.dBvals.as<float>(), c.dCnt.as<int>(),
+                                       c.dTau.as<uint2>(), flags.as<unsigned>(), c.stream));
+  } else {
+    CUDA_TRY(launch_stream_merge(Cc, c.top_m, c.wNewP.as<float>(), b, cur, n_del, c.dBids.as<int>(),
+                                 c.dBvals.as<float>(), c.stream));
+  }
   c.timer.mark("merge");
   // append the rows to the ring, growing it when full
   if (cur + b > c.cap_rows) {
@@ -503,6 +519,13 @@ int ceos_host::stream_update(ceos_stream* h, const float* Xn, int b, int n_del) 
   c.head = (c.head + n_del) % c.cap_rows;
   c.n_rows = cur + b - n_del;
   c.timer.mark("append");
+  if (c.reserve >= 0) {  // lists that fell below top_m: refill from all live rows
+    int refilled = 0;
+    ST_TRY(c.exact_refill(flags.as<unsigned>(), (int)std::min<long>(c.stride(), c.n_rows), c.stride(),
+                          c.dCnt.as<int>(), c.dTau.as<uint2>(), &refilled));
+    c.refilled_columns = refilled;
+    if (refilled) c.timer.mark("refill");
+  }
   CUDA_TRY(cudaStreamSynchronize(c.stream));
   c.timer.finish();
   if (log_level() >= 1) {
@@ -549,14 +572,89 @@ int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals) {
   if (!h || !ids || !vals) return fail(CEOS_ERR_ARG, "null argument");
   const Core& c = h->core;
   if (c.built != B_STREAM) return fail(CEOS_ERR_NOT_BUILT, "streamCEOs is not built");
-  const size_t cnt = (size_t)c.C() * 2 * c.top_m;
+  // the first top_m entries of each list (the bucket; lists hold stride() entries)
+  const size_t rows = (size_t)c.C() * 2, w = (size_t)c.top_m * 4, ld = (size_t)c.stride() * 4;
   CUDA_TRY(cudaSetDevice(c.device));
-  CUDA_TRY(cudaMemcpy(ids, c.dBids.p, cnt * 4, cudaMemcpyDeviceToHost));
-  CUDA_TRY(cudaMemcpy(vals, c.dBvals.p, cnt * 4, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy2D(ids, w, c.dBids.p, ld, w, rows, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy2D(vals, w, c.dBvals.p, ld, w, rows, cudaMemcpyDeviceToHost));
   return CEOS_OK;
 }
 
+int ceos_stream_set_reserve(ceos_stream* h, int reserve) {
+  if (!h) return fail(CEOS_ERR_ARG, "null handle");
+  if (h->core.attached) return fail(CEOS_ERR_BUSY, "the index is owned by a server");
+  if (h->core.built != B_NONE) return fail(CEOS_ERR_ARG, "set the reserve before build");
+  if (reserve < -1) return fail(CEOS_ERR_ARG, "reserve must be >= -1");
+  h->core.reserve = reserve;
+  return CEOS_OK;
+}
+
+int ceos_stream_get_reserve(const ceos_stream* h, int* reserve) {
+  if (!h || !reserve) return fail(CEOS_ERR_ARG, "null argument");
+  *reserve = h->core.reserve;
+  return CEOS_OK;
+}
+
+int ceos_stream_delete(ceos_stream* h, const int32_t* ids, int n_ids) {
+  if (!h) return fail(CEOS_ERR_ARG, "null handle");
+  if (h->core.attached) return fail(CEOS_ERR_BUSY, "the index is owned by a server");
+  return ceos_host::stream_delete(h, ids, n_ids);
+}
+
 }  // extern "C"
+
+int ceos_host::stream_delete(ceos_stream* h, const int32_t* ids, int n_ids) {
+  Core& c = h->core;
+  if (c.built != B_STREAM) return fail(CEOS_ERR_NOT_BUILT, "streamCEOs is not built");
+  if (c.reserve < 0)
+    return fail(CEOS_ERR_ARG, "random deletes need exact maintenance: call set_reserve before build");
+  if (n_ids < 0 || (n_ids > 0 && !ids)) return fail(CEOS_ERR_ARG, "bad id list");
+  std::vector<int> del(ids, ids + n_ids);
+  std::sort(del.begin(), del.end());
+  del.erase(std::unique(del.begin(), del.end()), del.end());
+  if (del.empty()) return CEOS_OK;
+  if (del.front() < 0 || del.back() >= c.n_rows)
+    return fail(CEOS_ERR_ARG, "ids must be in [0, %ld)", c.n_rows);
+  const long nd = (long)del.size();
+  if ((long)c.top_m > c.n_rows - nd)
+    return fail(CEOS_ERR_UPDATE_TOPM, "There is not enough indexed top-points for coCEOs after delete");
+  ST_TRY(c.ensure_device());
+  c.timer.begin(c.stream);
+  const int Cc = c.C(), M = c.stride();
+  DevBuf dDel, flags, nx;
+  CUDA_TRY(dDel.ensure((size_t)nd * 4));
+  CUDA_TRY(cudaMemcpyAsync(dDel.p, del.data(), nd * 4, cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(flags.ensure((size_t)Cc * 2 * 4));
+  CUDA_TRY(launch_stream_delete(Cc, M, c.top_m, dDel.as<int>(), (int)nd, c.dBids.as<int>(),
+                                c.dBvals.as<float>(), c.dCnt.as<int>(), c.dTau.as<uint2>(),
+                                flags.as<unsigned>(), c.stream));
+  c.timer.mark("buckets");
+  // compact the surviving rows into a fresh ring (same capacity, head 0)
+  CUDA_TRY(nx.ensure((size_t)c.cap_rows * c.ldx * 4));
+  CUDA_TRY(launch_compact_rows(c.dX.as<float>(), c.head, c.cap_rows, c.n_rows, c.ldx, dDel.as<int>(),
+                               (int)nd, nx.as<float>(), c.stream));
+  CUDA_TRY(cudaStreamSynchronize(c.stream));
+  c.dX.swap(nx);
+  nx.release();
+  c.head = 0;
+  c.n_rows -= nd;
+  if (c.xb_valid) {
+    CUDA_TRY(launch_to_bf16(c.dX.as<float>(), c.n_rows * (long)c.ldx, c.dXb.as<uint16_t>(), c.stream));
+  }
+  c.timer.mark("rows");
+  int refilled = 0;
+  ST_TRY(c.exact_refill(flags.as<unsigned>(), (int)std::min<long>(M, c.n_rows), M, c.dCnt.as<int>(),
+                        c.dTau.as<uint2>(), &refilled));
+  c.timer.mark("refill");
+  CUDA_TRY(cudaStreamSynchronize(c.stream));
+  c.timer.finish();
+  c.refilled_columns = refilled;
+  if (log_level() >= 1) {
+    std::printf("n_points (after delete): %ld\nrefilled columns: %d\n", c.n_rows, refilled);
+    print_timings("streamCEOs delete", c.timer);
+  }
+  return CEOS_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free search.
@@ -616,7 +714,7 @@ extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float*
   q.C = c.C();
   q.s = c.s;
   q.p = c.p;
-  q.m = c.top_m;
+  q.m = c.stride();
   q.c = c.c;
   q.k = k;
   q.X = c.dX.as<float>();

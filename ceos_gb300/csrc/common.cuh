@@ -35,6 +35,20 @@ CEOS_DEV uint64_t pack_key_u(uint32_t vkey, int id) {
   return ((uint64_t)vkey << 32) | (uint64_t)(0xffffffffu - (uint32_t)id);
 }
 CEOS_DEV int key_id(uint64_t k) { return (int)(0xffffffffu - (uint32_t)(k & 0xffffffffu)); }
+
+// Completeness threshold of an exactly maintained bucket list (x = fkey of the
+// value, y = id as a signed int): every live point outside the list ranks below
+// it, so list entries that rank at or above it are the exact top of the live
+// set. kTauNone certifies everything (the list holds every live point).
+constexpr uint32_t kTauNoneId = 0x7fffffffu;
+CEOS_DEV uint2 tau_none() { return make_uint2(0u, kTauNoneId); }
+CEOS_DEV bool tau_is_none(uint2 t) { return t.x == 0u && t.y == kTauNoneId; }
+CEOS_DEV uint2 tau_of(float v, int id) { return make_uint2(fkey(v), (uint32_t)id); }
+// (v, id) ranks at or above the threshold
+CEOS_DEV bool tau_certifies(uint2 t, float v, int id) {
+  const uint32_t k = fkey(v);
+  return k > t.x || (k == t.x && id <= (int)t.y);
+}
 CEOS_DEV float key_val(uint64_t k) { return fkey_inv((uint32_t)(k >> 32)); }
 
 // ---------------------------------------------------------------------------

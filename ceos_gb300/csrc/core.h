@@ -198,8 +198,16 @@ struct Core {
   DevBuf wStage, wQ, wQproj, wIds, wD, wTable, wProbes, wEst, wNewP, wNewX;
   Timer timer;
   int attached = 0;  // a serving loop owns the index (serve.cu)
+  // streamCEOs maintenance: -1 = the reference's (FIFO update refilled from
+  // new points only); >= 0 = exact, each column end keeping its best
+  // top_m + reserve live points (cnt valid in dCnt) so that random deletes can
+  // be absorbed, refilled from all live points when a list drops below top_m.
+  int reserve = -1;
+  DevBuf dCnt, dTau;
 
   int C() const { return n_proj * n_repeats; }
+  // entries stored per column end (the bucket list stride)
+  int stride() const { return top_m + (reserve > 0 ? reserve : 0); }
 
   void set_param(int D, int R, int m, int t, int sd) {
     n_proj = D;
@@ -239,7 +247,7 @@ struct Core {
 
   void release_all() {
     DevBuf* bufs[] = {&dX, &dSigns, &dP, &dBids, &dBvals, &dXb, &wStage, &wQ, &wQproj, &wIds,
-                      &wD, &wTable, &wProbes, &wEst, &wNewP, &wNewX};
+                      &wD, &wTable, &wProbes, &wEst, &wNewP, &wNewX, &dCnt, &dTau};
     xb_valid = false;
     for (DevBuf* b : bufs) b->release();
     built = B_NONE;
@@ -304,12 +312,14 @@ struct Core {
     return a;
   }
 
-  // Two-ended top-m buckets of the n_rows rows held in dX (see select.cu).
+  // Two-ended top-m buckets of the n_rows rows held in dX (see select.cu);
+  // m = stride() entries per column end.
   int build_buckets() {
     const long n = n_rows;
-    const int m = top_m, Cc = C();
-    if (m < 1 || m > n) return fail(CEOS_ERR_ARG, "top_m (%d) must be in [1, n_points=%ld]", m, n);
-    if (m > 8192) return fail(CEOS_ERR_UNSUPPORTED, "top_m > 8192 is not supported");
+    const int m = stride(), Cc = C();
+    if (m < 1 || m > n)
+      return fail(CEOS_ERR_ARG, "top_m (+ reserve) (%d) must be in [1, n_points=%ld]", m, n);
+    if (m > 8192) return fail(CEOS_ERR_UNSUPPORTED, "top_m (+ reserve) > 8192 is not supported");
     // ---- sample thresholds ----
     long S = n <= 65536 ? n : std::max(8192L, std::min(n / 8, 32L * m));
     if (S > n) S = n;
@@ -367,46 +377,58 @@ struct Core {
     samp.release();
     cand.release();
     // ---- exact fallback for flagged column ends ----
+    ST_TRY(exact_refill(failb.as<unsigned>(), m, m, nullptr, nullptr, &fallback_columns));
+    if (fallback_columns) timer.mark("exact-fallback");
+    return CEOS_OK;
+  }
+
+  // Exact top-msel over all n_rows rows for the column ends flagged in
+  // d_flags ([C][2]): the flagged columns are projected for every row
+  // (column-major dump, at most 2 GB at a time) and selected exactly, written
+  // at stride lds; d_cnt[end] = msel when given. Synchronizes the stream.
+  int exact_refill(const unsigned* d_flags, int msel, int lds, int* d_cnt, uint2* d_tau,
+                   int* n_cols_out) {
+    const long n = n_rows;
+    const int Cc = C();
     std::vector<unsigned> hf((size_t)Cc * 2);
-    CUDA_TRY(cudaMemcpyAsync(hf.data(), failb.p, hf.size() * 4, cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaMemcpyAsync(hf.data(), d_flags, hf.size() * 4, cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
     std::vector<int> failed_cols;
     for (int col = 0; col < Cc; ++col)
       if (hf[2 * col] || hf[2 * col + 1]) failed_cols.push_back(col);
-    fallback_columns = (int)failed_cols.size();
-    if (!failed_cols.empty()) {
-      const size_t budget = (size_t)2 << 30;
-      long per = std::max(1L, (long)(budget / ((size_t)n * 4)));
-      DevBuf dump, colslot, colofslot;
-      CUDA_TRY(colslot.ensure((size_t)Cc * 4));
-      for (size_t b0 = 0; b0 < failed_cols.size(); b0 += per) {
-        const int cnt_cols = (int)std::min((long)failed_cols.size() - (long)b0, per);
-        std::vector<int> cs(Cc, -1), cos(cnt_cols);
-        for (int i = 0; i < cnt_cols; ++i) {
-          cs[failed_cols[b0 + i]] = i;
-          cos[i] = failed_cols[b0 + i];
-        }
-        CUDA_TRY(dump.ensure((size_t)cnt_cols * n * 4));
-        CUDA_TRY(colofslot.ensure((size_t)cnt_cols * 4));
-        CUDA_TRY(cudaMemcpyAsync(colslot.p, cs.data(), Cc * 4, cudaMemcpyHostToDevice, stream));
-        CUDA_TRY(cudaMemcpyAsync(colofslot.p, cos.data(), cnt_cols * 4, cudaMemcpyHostToDevice, stream));
-        ProjArgs f = proj_base();
-        f.n_rows = n;
-        f.out = dump.as<float>();
-        f.ld_out = n;
-        f.col_slot = colslot.as<int>();
-        CUDA_TRY(launch_project(f, PROJ_COLS, L, sms, stream));
-        CUDA_TRY(launch_exact_buckets(dump.as<float>(), n, n, cnt_cols, colofslot.as<int>(),
-                                      failb.as<unsigned>(), m, dBids.as<int>(), dBvals.as<float>(),
-                                      stream));
-        CUDA_TRY(cudaStreamSynchronize(stream));
+    if (n_cols_out) *n_cols_out = (int)failed_cols.size();
+    if (failed_cols.empty()) return CEOS_OK;
+    const size_t budget = (size_t)2 << 30;
+    long per = std::max(1L, (long)(budget / ((size_t)n * 4)));
+    DevBuf dump, colslot, colofslot;
+    CUDA_TRY(colslot.ensure((size_t)Cc * 4));
+    for (size_t b0 = 0; b0 < failed_cols.size(); b0 += per) {
+      const int cnt_cols = (int)std::min((long)failed_cols.size() - (long)b0, per);
+      std::vector<int> cs(Cc, -1), cos(cnt_cols);
+      for (int i = 0; i < cnt_cols; ++i) {
+        cs[failed_cols[b0 + i]] = i;
+        cos[i] = failed_cols[b0 + i];
       }
-      timer.mark("exact-fallback");
+      CUDA_TRY(dump.ensure((size_t)cnt_cols * n * 4));
+      CUDA_TRY(colofslot.ensure((size_t)cnt_cols * 4));
+      CUDA_TRY(cudaMemcpyAsync(colslot.p, cs.data(), Cc * 4, cudaMemcpyHostToDevice, stream));
+      CUDA_TRY(cudaMemcpyAsync(colofslot.p, cos.data(), cnt_cols * 4, cudaMemcpyHostToDevice, stream));
+      ProjArgs f = proj_base();
+      f.n_rows = n;
+      f.out = dump.as<float>();
+      f.ld_out = n;
+      f.col_slot = colslot.as<int>();
+      CUDA_TRY(launch_project(f, PROJ_COLS, L, sms, stream));
+      CUDA_TRY(launch_exact_buckets(dump.as<float>(), n, n, cnt_cols, colofslot.as<int>(), d_flags,
+                                    msel, lds, dBids.as<int>(), dBvals.as<float>(), d_cnt, d_tau,
+                                    stream));
+      CUDA_TRY(cudaStreamSynchronize(stream));
     }
     return CEOS_OK;
   }
 
   int fallback_columns = 0;
+  int refilled_columns = 0;  // column ends refilled by the last exact update / delete
 
   // Bfloat16 copy of the whole row ring for the split-precision scan, made
   // on the first split search after a build and kept current by updates.
@@ -457,7 +479,7 @@ struct Core {
     q.C = C();
     q.s = s;
     q.p = p;
-    q.m = top_m;
+    q.m = stride();
     q.c = c;
     q.k = k;
     q.X = dX.as<float>();
@@ -467,7 +489,7 @@ struct Core {
     q.bids = dBids.as<int>();
     q.bvals = dBvals.as<float>();
     q.P = dP.as<float>();
-    q.distinct_ids = built == B_STREAM ? 0 : 1;
+    q.distinct_ids = (built != B_STREAM || reserve >= 0) ? 1 : 0;
     if (precision == CEOS_PRECISION_SPLIT_BF16) {
       q.Xb = dXb.as<uint16_t>();
       q.rescore = 4 * k;
@@ -598,4 +620,6 @@ namespace ceos_host {
 // streamCEOs::update (src/streamCEOs.cpp:174-369) on a built stream index;
 // defined in capi.cu, shared by ceos_stream_update and the serving loop.
 int stream_update(ceos_stream* h, const float* Xn, int b, int n_del);
+// Random-id deletes under exact maintenance; defined in capi.cu.
+int stream_delete(ceos_stream* h, const int32_t* ids, int n_ids);
 }  // namespace ceos_host

@@ -40,10 +40,15 @@ cudaError_t launch_sample_thresholds(const float* samp, long S, int C, int rank,
 // Per column end: top-m of the emitted candidates -> buckets; flags failures.
 cudaError_t launch_finish_buckets(const uint64_t* cand, const unsigned* cnt, int cap, int C, int m,
                                   int* bids, float* bvals, unsigned* fail, cudaStream_t st);
-// Exact top-m of dumped full columns (fallback): vals [slots][ld] -> buckets of col_of_slot.
+// Exact top-m of dumped full columns (fallback / refill): vals [slots][ld] -> the
+// flagged ends of col_of_slot's bucket lists (stride lds), cnt[end] = m and the
+// completeness threshold tau[end] if given.
 cudaError_t launch_exact_buckets(const float* vals, long n, long ld, int n_slots,
-                                 const int* col_of_slot, const unsigned* fail, int m, int* bids,
-                                 float* bvals, cudaStream_t st);
+                                 const int* col_of_slot, const unsigned* fail, int m, int lds,
+                                 int* bids, float* bvals, int* cnt, uint2* tau, cudaStream_t st);
+// Completeness thresholds of freshly built lists of M entries over n rows.
+cudaError_t launch_init_tau(int C, int M, long n, const int* bids, const float* bvals, uint2* tau,
+                            cudaStream_t st);
 
 // ---- queries (query.cu) ----
 struct QueryArgs {
@@ -101,6 +106,23 @@ cudaError_t launch_dense_select_rerank(const QueryArgs& a, int q0, int nq_chunk,
 // ---- streaming (stream.cu) ----
 cudaError_t launch_stream_merge(int C, int m, const float* newP, long b, long cur, int n_del,
                                 int* bids, float* bvals, cudaStream_t st);
+// Exact maintenance (lists of up to M = top_m + reserve entries, cnt valid per end,
+// completeness threshold tau per end): merge the entries surviving the FIFO delete
+// with the new points, keep the best M that rank at or above tau; flag[end] = 1
+// when fewer than m remain.
+cudaError_t launch_stream_merge_exact(int C, int M, int m, const float* newP, long b, long cur,
+                                      int n_del, int* bids, float* bvals, int* cnt, uint2* tau,
+                                      unsigned* flag, cudaStream_t st);
+// Random deletes: drop entries whose id is in del (sorted, distinct, nd ids), shift
+// the other ids down by the number of deleted ids below them, keep list order;
+// flag[end] = 1 when fewer than m remain.
+cudaError_t launch_stream_delete(int C, int M, int m, const int* del, int nd, int* bids,
+                                 float* bvals, int* cnt, uint2* tau, unsigned* flag,
+                                 cudaStream_t st);
+// Row compaction of the ring after random deletes: dst row j (stride ldx) = the
+// j-th surviving row of the ring (head, cap) of n rows.
+cudaError_t launch_compact_rows(const float* X, long head, long cap, long n, int ldx,
+                                const int* del, int nd, float* dst, cudaStream_t st);
 
 // ---- misc ----
 cudaError_t launch_pad_rows(const float* src, long n, int d, float* dst, int ldx, cudaStream_t st);

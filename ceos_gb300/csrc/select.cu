@@ -93,10 +93,14 @@ cudaError_t launch_finish_buckets(const uint64_t* cand, const unsigned* cnt, int
   return cudaGetLastError();
 }
 
-// Exact selection over a full dumped column (rows 0..n-1 of slot).
+// Exact selection over a full dumped column (rows 0..n-1 of slot): the best
+// m of the column end, written at stride `lds` (>= m) of the bucket lists,
+// and m into cnt[column end] when cnt is given, with the list's completeness
+// threshold (its last entry, or none when the list holds all n rows) into tau.
 __global__ void __launch_bounds__(512) k_exact_buckets(const float* vals, long n, long ld,
                                                       const int* col_of_slot, const unsigned* fail,
-                                                      int m, int* bids, float* bvals) {
+                                                      int m, int lds, int* bids, float* bvals,
+                                                      int* cnt, uint2* tau) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint32_t scratch[16];
   const int out_cap = next_pow2(m);
@@ -118,19 +122,39 @@ __global__ void __launch_bounds__(512) k_exact_buckets(const float* vals, long n
       n, m, s_out, out_cap, hist, maybe, kSelMaybe, scratch);
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const uint64_t k = s_out[i];
-    bids[ce * m + i] = key_id(k);
-    bvals[ce * m + i] = key_val(k);
+    bids[ce * lds + i] = key_id(k);
+    bvals[ce * lds + i] = key_val(k);
   }
+  if (cnt && threadIdx.x == 0) cnt[ce] = m;
+  if (tau && threadIdx.x == 0)
+    tau[ce] = (n > m) ? tau_of(key_val(s_out[m - 1]), key_id(s_out[m - 1])) : tau_none();
 }
 
 cudaError_t launch_exact_buckets(const float* vals, long n, long ld, int n_slots,
-                                 const int* col_of_slot, const unsigned* fail, int m, int* bids,
-                                 float* bvals, cudaStream_t st) {
+                                 const int* col_of_slot, const unsigned* fail, int m, int lds,
+                                 int* bids, float* bvals, int* cnt, uint2* tau, cudaStream_t st) {
   const size_t smem = sel_smem(m);
   cudaError_t e =
       cudaFuncSetAttribute(k_exact_buckets, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_exact_buckets<<<2 * n_slots, 512, smem, st>>>(vals, n, ld, col_of_slot, fail, m, bids, bvals);
+  k_exact_buckets<<<2 * n_slots, 512, smem, st>>>(vals, n, ld, col_of_slot, fail, m, lds, bids,
+                                                  bvals, cnt, tau);
+  return cudaGetLastError();
+}
+
+// Thresholds of freshly built lists: the last of the M entries, or none when
+// the list holds all n rows.
+__global__ void k_init_tau(long n_ends, int M, long n, const int* bids, const float* bvals,
+                           uint2* tau) {
+  for (long ce = (long)blockIdx.x * blockDim.x + threadIdx.x; ce < n_ends;
+       ce += (long)gridDim.x * blockDim.x)
+    tau[ce] = n > M ? tau_of(bvals[ce * M + M - 1], bids[ce * M + M - 1]) : tau_none();
+}
+
+cudaError_t launch_init_tau(int C, int M, long n, const int* bids, const float* bvals, uint2* tau,
+                            cudaStream_t st) {
+  const long ends = 2L * C;
+  k_init_tau<<<(unsigned)((ends + 255) / 256), 256, 0, st>>>(ends, M, n, bids, bvals, tau);
   return cudaGetLastError();
 }
 

@@ -38,12 +38,13 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-enum ReqKind { R_QUERY = 0, R_UPDATE = 1 };
+enum ReqKind { R_QUERY = 0, R_UPDATE = 1, R_DELETE = 2 };
 
 struct Request {
   uint64_t ticket = 0;
   int kind = R_QUERY;
   std::vector<float> data;  // queries (nq x d) or new rows (n_new x d)
+  std::vector<int32_t> del;  // ids of a delete
   int nq = 0, k = 0, s = 0, cap = 0;
   int n_new = 0, n_del = 0;
   int32_t* ids = nullptr;
@@ -331,7 +332,7 @@ struct ceos_server {
       std::unique_lock<std::mutex> lk(mu);
       if (!queue.empty()) {
         Request* head = queue.front();
-        if (head->kind == R_UPDATE) {
+        if (head->kind != R_QUERY) {
           if (!any_busy) {
             queue.pop_front();
             lk.unlock();
@@ -389,7 +390,9 @@ struct ceos_server {
 
 int ceos_server::run_update(Request* r) {
   if (!stream_handle) return fail(CEOS_ERR_ARG, "updates need a streamCEOs server");
-  const int st = ceos_host::stream_update(stream_handle, r->data.data(), r->n_new, r->n_del);
+  const int st = r->kind == R_DELETE
+                     ? ceos_host::stream_delete(stream_handle, r->del.data(), (int)r->del.size())
+                     : ceos_host::stream_update(stream_handle, r->data.data(), r->n_new, r->n_del);
   if (st != CEOS_OK) return st;
   ST_TRY(core->ensure_bf16());
   CUDA_TRY(cudaStreamSynchronize(core->stream));
@@ -580,6 +583,25 @@ int ceos_server_submit_update(ceos_server* s, const float* X_new, int n_new, int
   r->n_new = n_new;
   r->n_del = n_del;
   r->data.assign(X_new, X_new + (size_t)n_new * s->d);
+  std::unique_lock<std::mutex> lk(s->mu);
+  r->ticket = s->next_ticket++;
+  *ticket = r->ticket;
+  Request* raw = r.get();
+  s->reqs.emplace(raw->ticket, std::move(r));
+  s->queue.push_back(raw);
+  lk.unlock();
+  s->cv_work.notify_one();
+  return CEOS_OK;
+}
+
+int ceos_server_submit_delete(ceos_server* s, const int32_t* ids, int n_ids, uint64_t* ticket) {
+  if (!s || !ticket) return fail(CEOS_ERR_ARG, "null handle or ticket");
+  if (!s->stream_handle) return fail(CEOS_ERR_ARG, "deletes need a server over a streamCEOs index");
+  if (n_ids < 0 || (n_ids > 0 && !ids)) return fail(CEOS_ERR_ARG, "bad id list");
+  auto r = std::make_unique<Request>();
+  r->t_submit = Clock::now();
+  r->kind = R_DELETE;
+  r->del.assign(ids, ids + n_ids);
   std::unique_lock<std::mutex> lk(s->mu);
   r->ticket = s->next_ticket++;
   *ticket = r->ticket;

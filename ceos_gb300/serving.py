@@ -109,6 +109,15 @@ class Server:
         self._pending[t.value] = req
         return req
 
+    def submit_delete(self, ids) -> Request:
+        a = np.ascontiguousarray(np.asarray(ids, dtype=np.int32).ravel())
+        t = C.c_uint64()
+        _capi.check(self._L.ceos_server_submit_delete(self._h, a.ctypes.data if a.size else None,
+                                                      a.size, C.byref(t)))
+        req = Request(t.value)
+        self._pending[t.value] = req
+        return req
+
     def wait(self, req: Request, timeout: float | None = None):
         """Block until `req` completes; returns (ids, dists) for a query request."""
         ms = -1 if timeout is None else int(timeout * 1000)

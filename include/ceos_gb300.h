@@ -192,6 +192,20 @@ int ceos_stream_estimate_search(ceos_stream* h, const float* Q, int n_queries, i
 /* hash_search: python/python_wrapper.cpp:69-70 -> src/streamCEOs.cpp:621-877 */
 int ceos_stream_hash_search(ceos_stream* h, const float* Q, int n_queries, int n_neighbors,
                             int verbose, int32_t* ids, float* dists);
+/* Exact maintenance and random-id deletes (no reference counterpart: the reference
+ * deletes only from the front, n_delPoints of src/streamCEOs.cpp:207-208, and refills a
+ * bucket only from new points, leaving stale rows when too few remain, :337-352).
+ * set_reserve(r >= 0) before build keeps top_points + r entries per column end; every
+ * bucket is then the exact top-m over the live points after each update and delete
+ * (a list that drops below top_m is refilled from all live rows). -1 (default) keeps
+ * the reference's maintenance. */
+int ceos_stream_set_reserve(ceos_stream* h, int reserve);
+int ceos_stream_get_reserve(const ceos_stream* h, int* reserve);
+/* Delete the points with the given current ids (0 .. size-1, duplicates ignored);
+ * later ids move down, as erasing from the reference's deque would. Needs
+ * set_reserve(>= 0) before build. CEOS_ERR_UPDATE_TOPM when fewer than top_points
+ * points would remain. */
+int ceos_stream_delete(ceos_stream* h, const int32_t* ids, int n_ids);
 /* Current number of points (the reference's deque_X.size()). */
 int ceos_stream_size(const ceos_stream* h, int* n_points);
 int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals);
@@ -272,6 +286,8 @@ int ceos_server_submit(ceos_server* s, const float* Q, int n_queries, int n_neig
 /* streamCEOs update (src/streamCEOs.cpp:174-369) in queue order; rows copied at the call. */
 int ceos_server_submit_update(ceos_server* s, const float* X_new, int n_new, int n_del,
                               uint64_t* ticket);
+/* Random-id delete (ceos_stream_delete) in queue order; ids copied at the call. */
+int ceos_server_submit_delete(ceos_server* s, const int32_t* ids, int n_ids, uint64_t* ticket);
 /* Block until the request completes (timeout_ms < 0: no limit); returns its status,
  * CEOS_ERR_TIMEOUT if it is still running. A completed ticket is released. */
 int ceos_server_wait(ceos_server* s, uint64_t ticket, int timeout_ms);

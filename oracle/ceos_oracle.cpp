@@ -575,8 +575,46 @@ struct OracleStream {
   std::vector<float> B_vals;   // [C][2][m]
   std::vector<uint8_t> bits;
   bool built = false;
+  // Exact maintenance (the GPU library's random-delete extension): after every
+  // update or delete the buckets are the exact two-ended top-m over the live
+  // rows, recomputed here from scratch.
+  bool exact = false;
 
   explicit OracleStream(int d) : n_features(d) {}
+
+  void rebuild_exact() {
+    const int n = (int)X.size(), Cc = C();
+    std::vector<float> flat((size_t)n * n_features);
+    for (int i = 0; i < n; ++i) std::memcpy(&flat[(size_t)i * n_features], X[i].data(), n_features * sizeof(float));
+    std::vector<float> Pt((size_t)n * Cc);
+    project_rows(flat.data(), n, n_features, fhtDim, n_proj, n_repeats, bits.data(), Pt.data());
+    B_ids.assign((size_t)Cc * 2 * top_m, 0);
+    B_vals.assign((size_t)Cc * 2 * top_m, 0.0f);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int c = 0; c < Cc; ++c) {
+      size_t o = (size_t)c * 2 * top_m;
+      select_column(Pt.data() + c, n, Cc, top_m, &B_ids[o], &B_vals[o], &B_ids[o + top_m],
+                    &B_vals[o + top_m]);
+    }
+    n_points = n;
+  }
+
+  // Delete the rows with the given current ids (positions); later rows move
+  // down, as erasing from a deque would.
+  int delete_ids(const int* ids, int nd) {
+    if (!built) return ST_NOT_BUILT;
+    if (!exact) return ST_BAD_ARG;
+    std::vector<int> v(ids, ids + nd);
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    for (int id : v)
+      if (id < 0 || id >= (int)X.size()) return ST_BAD_ARG;
+    if (top_m > (int)X.size() - (int)v.size()) return ST_UPDATE_TOPM;
+    for (int i = (int)v.size() - 1; i >= 0; --i) X.erase(X.begin() + v[i]);
+    omp_set_num_threads(n_threads);
+    rebuild_exact();
+    return ST_OK;
+  }
 
   // src/streamCEOs.h:53-70: note n_probed_vectors (not n_probed_points) is
   // reset to top_m here.
@@ -630,6 +668,10 @@ struct OracleStream {
       X.emplace_back(newX + (size_t)i * n_features, newX + (size_t)(i + 1) * n_features);
     for (int i = 0; i < n_del; ++i) X.pop_front();
     n_points = (int)X.size();
+    if (exact) {
+      rebuild_exact();
+      return ST_OK;
+    }
     const int Cc = C(), m = top_m;
     std::vector<float> Pn((size_t)b * Cc);
     project_rows(newX, b, n_features, fhtDim, n_proj, n_repeats, bits.data(), Pn.data());
@@ -911,6 +953,8 @@ int orc_stream_build(void* h, const float* X, int n) { return ((OracleStream*)h)
 int orc_stream_update(void* h, const float* X, int b, int n_del) {
   return ((OracleStream*)h)->update(X, b, n_del);
 }
+void orc_stream_set_exact(void* h, int exact) { ((OracleStream*)h)->exact = exact != 0; }
+int orc_stream_delete(void* h, const int* ids, int n) { return ((OracleStream*)h)->delete_ids(ids, n); }
 int orc_stream_estimate_search(void* h, const float* Q, int nq, int k, int* ids, float* d) {
   return ((OracleStream*)h)->estimate_search(Q, nq, k, ids, d);
 }

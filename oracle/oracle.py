@@ -118,6 +118,9 @@ def lib():
             L.orc_stream_estimate_search.argtypes = [vp, _F32P, C.c_int, C.c_int, _I32P, _F32P]
             L.orc_stream_hash_search.argtypes = [vp, _F32P, C.c_int, C.c_int, _I32P, _F32P]
             L.orc_stream_get_buckets.argtypes = [vp, _I32P, _F32P]
+            L.orc_stream_set_exact.argtypes = [vp, C.c_int]
+            L.orc_stream_set_exact.restype = None
+            L.orc_stream_delete.argtypes = [vp, _I32P, C.c_int]
             _lib = L
     return _lib
 
@@ -373,6 +376,15 @@ class streamCEOs(_Attrs):
     def update(self, new_dataset, n_delPoints=0):
         X = _f32(new_dataset).reshape(-1, self.n_features)
         _check(self._L.orc_stream_update(self._h, X, X.shape[0], int(n_delPoints)))
+
+    def set_reserve(self, reserve: int):
+        """Exact maintenance (reserve >= 0): buckets recomputed over the live rows
+        after every update / delete (the GPU keeps top_m + reserve per list)."""
+        self._L.orc_stream_set_exact(self._h, 1 if int(reserve) >= 0 else 0)
+
+    def delete(self, ids):
+        ids = np.ascontiguousarray(np.asarray(ids, dtype=np.int32).ravel())
+        _check(self._L.orc_stream_delete(self._h, ids, ids.size))
 
     def _search(self, fn, Q, k):
         Q = _f32(Q)

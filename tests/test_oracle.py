@@ -150,3 +150,30 @@ def test_bf16_rounding_nearest_even(oracle):
     ref = (((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000) & 0xFFFFFFFF).astype(np.uint32).view(np.float32)
     got = oracle.bf16_round(x)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_oracle_exact_stream_equals_fresh_build(oracle):
+    """Exact maintenance (random-delete extension): after inserts and random
+    deletes the stream's buckets are the buckets of a coCEOs index built from
+    scratch on the live rows."""
+    d = 20
+    pool = netflix_like(1500, d, seed=12)
+    s = oracle.streamCEOs(d)
+    s.setIndexParam(32, 2, 15, 2, 9)
+    s.set_reserve(0)
+    s.build(pool[:600])
+    live = pool[:600]
+    s.update(pool[600:900], 50)
+    live = np.concatenate([live[50:], pool[600:900]])
+    dels = np.array([0, 5, 6, 100, 849])
+    s.delete(dels)
+    live = np.delete(live, dels, axis=0)
+    assert s.size == len(live)
+    f = oracle.CEOs(len(live), d)
+    f.setIndexParam(32, 2, 15, 2, 9)
+    f.build_coCEOs_Est(live)
+    a, b = s.buckets()
+    c, e = f.buckets()
+    assert np.array_equal(a, c) and np.array_equal(b, e)
+    with pytest.raises(ValueError):
+        s.delete([len(live)])
