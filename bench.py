@@ -166,6 +166,111 @@ def served_leg(args):
     return out
 
 
+# Streaming configuration: 500k x 300 start index (rows g * s, g ~ N(0, I/300),
+# s ~ LogNormal(0, 0.5)), then about 2M inserted rows in batches of U[1, 10000],
+# 0.1% of the live ids deleted at random after every batch, and query requests
+# of U[1, 128] queries between batches; exact maintenance with a reserve of
+# top_m / 2 entries per list.
+STREAM = dict(n0=500_000, d=300, D=1024, R=4, m=200, p=200, s=20, c=500, k=10, seed=42,
+              reserve=100, insert_rows=2_000_000, max_batch_rows=10_000, delete_frac=0.001,
+              query_requests_per_batch=4, max_request=128, stream_seed=7)
+
+
+def netflix_like(n, d, seed):
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, d), np.float32)
+    step = 250_000
+    for i in range(0, n, step):
+        j = min(n, i + step)
+        out[i:j] = rng.standard_normal((j - i, d), dtype=np.float32) / np.float32(np.sqrt(d))
+        out[i:j] *= rng.lognormal(0.0, 0.5, (j - i, 1)).astype(np.float32)
+    return out
+
+
+def stream_leg(args):
+    """streamCEOs at scale through the serving loop, batch by batch: insert,
+    random delete, query requests; insert/delete throughput, query latency,
+    recall@10 over the live rows against the GPU FP64 ground truth, and the
+    final buckets compared with a fresh build on the live rows."""
+    import ceos_gb300.CEOs as CEOs
+    from ceos_gb300 import _capi
+    from ceos_gb300.serving import Server
+
+    cfg = STREAM
+    d = cfg["d"]
+    rng = np.random.default_rng(cfg["stream_seed"])
+    sizes = []
+    tot = 0
+    while tot < cfg["insert_rows"]:
+        b = int(rng.integers(1, cfg["max_batch_rows"] + 1))
+        sizes.append(b)
+        tot += b
+    X_all = netflix_like(cfg["n0"] + tot, d, 21)
+    pool = netflix_like(20_000, d, 22) * np.float32(np.sqrt(d))  # N(0, I)-scale queries
+    st = CEOs.streamCEOs(d)
+    st.setIndexParam(cfg["D"], cfg["R"], cfg["m"], -1, cfg["seed"])
+    st.set_reserve(cfg["reserve"])
+    t0 = time.perf_counter()
+    st.build(X_all[:cfg["n0"]])
+    build_s = time.perf_counter() - t0
+    st.n_probed_vectors, st.n_probed_points, st.n_cand = cfg["s"], cfg["p"], cfg["c"]
+    live = np.arange(cfg["n0"], dtype=np.int64)  # global row index of every current id
+    srv = Server(st, algo="estimate", n_slots=4, max_batch=256, max_neighbors=cfg["k"],
+                 max_probed_vectors=cfg["s"])
+    warm = srv.submit(pool[:64], cfg["k"], cfg["s"])
+    srv.wait(warm)
+    srv.reset_stats()
+    pos = cfg["n0"]
+    t_ins = t_del = 0.0
+    n_del_total = 0
+    n_queries = 0
+    t_start = time.perf_counter()
+    for b in sizes:
+        t = time.perf_counter()
+        srv.wait(srv.submit_update(X_all[pos:pos + b]))
+        t_ins += time.perf_counter() - t
+        live = np.concatenate([live, np.arange(pos, pos + b)])
+        pos += b
+        nd = max(1, int(round(cfg["delete_frac"] * len(live))))
+        dels = rng.choice(len(live), size=nd, replace=False).astype(np.int32)
+        t = time.perf_counter()
+        srv.wait(srv.submit_delete(dels))
+        t_del += time.perf_counter() - t
+        live = np.delete(live, dels)
+        n_del_total += nd
+        reqs = []
+        for _ in range(cfg["query_requests_per_batch"]):
+            nq = int(rng.integers(1, cfg["max_request"] + 1))
+            o = int(rng.integers(0, len(pool) - nq))
+            reqs.append(srv.submit(pool[o:o + nq], cfg["k"], cfg["s"]))
+            n_queries += nq
+        for r in reqs:
+            srv.wait(r)
+    wall = time.perf_counter() - t_start
+    stats = srv.stats()
+    # recall@10 over the live rows
+    Qr = pool[:500]
+    ids, _ = srv.wait(srv.submit(Qr, cfg["k"], cfg["s"]))
+    srv.close()
+    Xlive = X_all[live]
+    gt, _ = _capi.bruteforce_fp64(Xlive, Qr, cfg["k"])
+    rec = float(np.mean([len(np.intersect1d(a, g)) / cfg["k"] for a, g in zip(ids, gt)]))
+    # size-independent property: the maintained buckets equal a fresh build
+    fresh = CEOs.CEOs(len(live), d)
+    fresh.setIndexParam(cfg["D"], cfg["R"], cfg["m"], -1, cfg["seed"])
+    fresh.build_coCEOs_Est(Xlive)
+    fi, fv = fresh.buckets()
+    si, sv = st.buckets()
+    same = bool(np.array_equal(fi, si) and np.array_equal(fv.view(np.uint32), sv.view(np.uint32)))
+    return {"config": dict(cfg), "batches": len(sizes), "inserted_rows": int(tot),
+            "deleted_ids": int(n_del_total), "final_size": int(st.size), "build_s": build_s,
+            "insert_rows_per_s": tot / t_ins, "delete_ids_per_s": n_del_total / t_del,
+            "wall_s": wall, "query_requests": stats["requests"], "queries": n_queries,
+            "query_p50_ms": stats["p50_ms"], "query_p99_ms": stats["p99_ms"],
+            "recall@10_live": rec, "recall_queries": len(Qr),
+            "buckets_equal_fresh_build": same}
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -340,16 +445,17 @@ def main():
     ap.add_argument("--ref-queries", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--recall-queries", type=int, default=200)
-    ap.add_argument("--only", choices=["served"], default=None,
+    ap.add_argument("--only", choices=["served", "stream"], default=None,
                     help="run one secondary leg alone and print its JSON")
     ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     os.environ.setdefault("CEOS_GB300_LOG", "0")
-    if args.only == "served":
+    if args.only in ("served", "stream"):
         from ceos_gb300 import _capi
 
         _capi.lib().ceos_set_log_level(0)
-        print(json.dumps({"served": served_leg(args)}))
+        leg = served_leg(args) if args.only == "served" else stream_leg(args)
+        print(json.dumps({args.only: leg}))
         return 0
 
     X = sift_like(CFG["n"], CFG["d"], 7)
