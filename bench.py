@@ -271,6 +271,61 @@ def stream_leg(args):
             "buckets_equal_fresh_build": same}
 
 
+# Split-precision configuration: GIST-shaped 1M x 960 index, 1000 queries.
+SPLIT = dict(n=1_000_000, d=960, nq=1000, D=1024, R=8, m=1000, s=60, c=4000, k=10, seed=42)
+
+
+def gist_like(n, d, seed):
+    """|N(0,1)| * 0.05 with row norms scaled by LogNormal(0, 0.3)."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, d), np.float32)
+    step = 100_000
+    for i in range(0, n, step):
+        j = min(n, i + step)
+        v = np.abs(rng.standard_normal((j - i, d), dtype=np.float32)) * np.float32(0.05)
+        out[i:j] = v * rng.lognormal(0.0, 0.3, (j - i, 1)).astype(np.float32)
+    return out
+
+
+def split_leg(args):
+    """FP32 vs split-BF16 on the 1M x 960 index: build time, search queries/s
+    (device time, queries resident), recall@10 and the largest relative error of
+    the reported scores against the GPU FP64 ground truth."""
+    import ceos_gb300.CEOs as CEOs
+    from ceos_gb300 import _capi
+
+    cfg = SPLIT
+    X = gist_like(cfg["n"], cfg["d"], 3)
+    Q = gist_like(cfg["nq"], cfg["d"], 4)
+    gt, gts = _capi.bruteforce_fp64(X, Q, cfg["k"])
+    out = {"config": dict(cfg)}
+    for prec in ("fp32", "split_bf16"):
+        idx = CEOs.CEOs(cfg["n"], cfg["d"])
+        idx.setIndexParam(cfg["D"], cfg["R"], cfg["m"], -1, cfg["seed"])
+        idx.precision = prec
+        builds = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            idx.build_coCEOs_Est(X)
+            builds.append((time.perf_counter() - t0, idx.last_timings()))
+        idx.n_probed_vectors, idx.n_cand = cfg["s"], cfg["c"]
+        ms = []
+        for i in range(args.warmup + max(3, args.steps // 3)):
+            ids, dists = idx.search_coCEOs_Est(Q, cfg["k"])
+            t = idx.last_timings()
+            if i >= args.warmup:
+                ms.append(t["estimate+rerank"] + t["project"])
+        rec = float(np.mean([len(np.intersect1d(a, b)) / cfg["k"] for a, b in zip(ids, gt)]))
+        # reported scores vs the FP64 inner products of the reported ids
+        exact = np.einsum("qkd,qd->qk", X[ids].astype(np.float64), Q.astype(np.float64))
+        err = float(np.max(np.abs(dists - exact) / np.maximum(np.abs(exact), 1e-30)))
+        out[prec] = {"build_s": builds[-1][0], "build_phases_ms": builds[-1][1],
+                     "queries_per_s": cfg["nq"] / (float(np.mean(ms)) / 1e3),
+                     "recall@10": rec, "max_rel_score_err": err}
+    out["split_vs_fp32_qps"] = out["split_bf16"]["queries_per_s"] / out["fp32"]["queries_per_s"]
+    return out
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -445,16 +500,16 @@ def main():
     ap.add_argument("--ref-queries", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--recall-queries", type=int, default=200)
-    ap.add_argument("--only", choices=["served", "stream"], default=None,
+    ap.add_argument("--only", choices=["served", "stream", "split"], default=None,
                     help="run one secondary leg alone and print its JSON")
     ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     os.environ.setdefault("CEOS_GB300_LOG", "0")
-    if args.only in ("served", "stream"):
+    if args.only:
         from ceos_gb300 import _capi
 
         _capi.lib().ceos_set_log_level(0)
-        leg = served_leg(args) if args.only == "served" else stream_leg(args)
+        leg = {"served": served_leg, "stream": stream_leg, "split": split_leg}[args.only](args)
         print(json.dumps({args.only: leg}))
         return 0
 
