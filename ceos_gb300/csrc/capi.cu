@@ -137,6 +137,7 @@ static int index_build_common(ceos_index* h, const float* X, const char* what) {
   CUDA_TRY(c.dX.ensure((size_t)c.n_rows * c.ldx * 4));
   ST_TRY(c.upload_rows(X, c.n_rows, c.dX.as<float>()));
   ST_TRY(c.upload_signs());
+  c.proj_tensor = (c.precision == CEOS_PRECISION_SPLIT_BF16 && project_tc_supported(c.L)) ? 1 : 0;
   c.timer.mark("h2d");
   if (log_level() >= 1) {
     std::printf("%s\nn_points: %ld\nn_features: %d\nn_repeats: %d\nn_proj: %d\ntop_m: %d\nfhtDim: %d\n",
@@ -405,6 +406,7 @@ int ceos_stream_build(ceos_stream* h, const float* X, int n_points) {
   CUDA_TRY(c.dX.ensure((size_t)c.cap_rows * c.ldx * 4));
   ST_TRY(c.upload_rows(X, c.n_rows, c.dX.as<float>()));
   ST_TRY(c.upload_signs());
+  c.proj_tensor = (c.precision == CEOS_PRECISION_SPLIT_BF16 && project_tc_supported(c.L)) ? 1 : 0;
   c.timer.mark("h2d");
   if (log_level() >= 1)
     std::printf("n_features: %d\nn_proj: %d\ntop_m: %d\nfhtDim: %d\nn_points: %ld\n", c.n_features,

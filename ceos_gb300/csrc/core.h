@@ -204,6 +204,10 @@ struct Core {
   // be absorbed, refilled from all live points when a list drops below top_m.
   int reserve = -1;
   DevBuf dCnt, dTau;
+  // transform of the built index: 1 = split-precision tensor-core FWHT, taken
+  // from the precision at build time and used for every later projection
+  // (queries, updates) so that query and bucket projections agree
+  int proj_tensor = 0;
 
   int C() const { return n_proj * n_repeats; }
   // entries stored per column end (the bucket list stride)
@@ -309,6 +313,7 @@ struct Core {
     a.D = n_proj;
     a.R = n_repeats;
     a.signs = dSigns.as<uint32_t>();
+    a.tensor = proj_tensor;
     return a;
   }
 

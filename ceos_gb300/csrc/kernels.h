@@ -29,9 +29,14 @@ struct ProjArgs {
   int cap = 0;
   long id_base = 0;
   const unsigned char* col_active = nullptr;  // optional per-column enable
+  // 1 = split-precision tensor-core transform (project_tc.cu) where supported
+  int tensor = 0;
 };
 
 cudaError_t launch_project(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st);
+// Split-precision tensor-core projection (fhtDim 256 and 1024).
+bool project_tc_supported(int L);
+cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st);
 
 // ---- selection (select.cu) ----
 // Per column: u32 thresholds so that about `rank` sample values pass each end.

@@ -22,6 +22,7 @@ cudaError_t launch_project_L(const ProjArgs& a, int mode, int num_sms, cudaStrea
 
 cudaError_t launch_project(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st) {
   if (a.n_rows <= 0) return cudaSuccess;
+  if (a.tensor && project_tc_supported(L)) return launch_project_tc(a, mode, L, num_sms, st);
   switch (L) {
     case 1: return launch_project_L<1>(a, mode, num_sms, st);
     case 2: return launch_project_L<2>(a, mode, num_sms, st);

@@ -71,6 +71,8 @@ def test_server_mix_equals_alone(gpu, oracle, algo, precision):
     assert srv1.stats()["graph_launches"] == 0
     srv1.close()
     _same(alone[:12], one)
+    if precision != "fp32":
+        return  # split precision builds with the tensor-core transform: no bit-exact oracle
     # the oracle, on a few requests
     o = oracle.CEOs(n, d)
     o.setIndexParam(256, 2, 150, 8, 42)
