@@ -170,4 +170,43 @@ CEOS_DEV void fwht_round(const float* src, float* dst, const uint32_t* sw, int l
   __syncwarp();
 }
 
+// Round 0 with its input in registers (phase-0 line layout: task t of the
+// lane holds the E contiguous elements of line lane + 32 t), output to dst.
+// Used when the phase-0 lines of a lane fit in 32 registers, so the input row
+// needs no shared-memory copy.
+template <int L>
+struct RegRow {
+  static constexpr int E = 1 << FwhtCfg<L>::bits(0);
+  static constexpr int T = FwhtCfg<L>::tasks(0);
+  static constexpr bool ok = E * T <= 32 && E >= 4;
+};
+
+template <int L>
+CEOS_DEV void fwht_round_regs(const float (&x)[RegRow<L>::T][RegRow<L>::E], float* dst,
+                              const uint32_t* sw, int lane) {
+  using Cfg = FwhtCfg<L>;
+  constexpr int B = Cfg::bits(0);
+  constexpr int E = 1 << B;
+  constexpr int lines0 = Cfg::F / E;
+#pragma unroll
+  for (int t = 0; t < RegRow<L>::T; ++t) {
+    const int task = lane + 32 * t;
+    const int vec = task / lines0;
+    const int line = task % lines0;
+    const int j0 = line * E;
+    float* d = dst + vec * Cfg::Vstride + padj(j0);
+    const uint32_t nword = ~(sw[j0 >> 5] >> (j0 & 31));  // bit e set => flip
+    float v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      v[e] = __uint_as_float(__float_as_uint(x[t][e]) ^ ((nword << (31 - e)) & 0x80000000u));
+    reg_stages<B>(v);
+#pragma unroll
+    for (int k = 0; k < E / 4; ++k)
+      reinterpret_cast<float4*>(d)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+  }
+  if constexpr (Cfg::P > 1) fwht_phase<L, 1>(dst, lane);
+  __syncwarp();
+}
+
 }  // namespace ceos

@@ -29,9 +29,14 @@ constexpr int proj_warps() {
   return L >= 12 ? 4 : 8;
 }
 
+// When a lane's phase-0 lines fit in registers (RegRow<L>::ok: F = 256, 1024
+// and below), the input rows are loaded straight into registers in that
+// layout and round 0 starts from them; each warp then needs a single
+// shared-memory buffer, which leaves L1 room for the candidate thresholds.
 template <int L, int MODE>
-__global__ void __launch_bounds__(256) k_project(ProjArgs a) {
+__global__ void __launch_bounds__(256, RegRow<L>::ok ? 3 : 1) k_project(ProjArgs a) {
   using Cfg = FwhtCfg<L>;
+  constexpr bool kRegRow = RegRow<L>::ok;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int words = Cfg::words;
   uint32_t* s_signs = reinterpret_cast<uint32_t*>(smem_raw);
@@ -44,14 +49,43 @@ __global__ void __launch_bounds__(256) k_project(ProjArgs a) {
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int warps_per_block = blockDim.x >> 5;
-  float* xbuf = s_vec + (size_t)warp * 2 * Cfg::V * Cfg::Vstride;
-  float* wbuf = xbuf + Cfg::V * Cfg::Vstride;
+  constexpr int kBufs = kRegRow ? 1 : 2;
+  float* xbuf = s_vec + (size_t)warp * kBufs * Cfg::V * Cfg::Vstride;
+  float* wbuf = xbuf + (kBufs - 1) * Cfg::V * Cfg::Vstride;
   const int C = a.R * a.D;
 
   const long n_groups = (a.n_rows + Cfg::V - 1) / Cfg::V;
   for (long g = (long)blockIdx.x * warps_per_block + warp; g < n_groups;
        g += (long)gridDim.x * warps_per_block) {
     const long row0 = g * Cfg::V;
+    float xr[RegRow<L>::T][RegRow<L>::E];
+    if constexpr (kRegRow) {
+      // ---- load V rows (zero padded to F) into the phase-0 register layout ----
+      constexpr int E = RegRow<L>::E, lines0 = Cfg::F / E;
+#pragma unroll
+      for (int t = 0; t < RegRow<L>::T; ++t) {
+        const int task = lane + 32 * t;
+        const int v = task / lines0;
+        const int j0 = (task % lines0) * E;
+        const long row = row0 + v;
+        const float4* src = nullptr;
+        if (row < a.n_rows) {
+          long r = a.row_map ? a.row_map[row] : row;
+          r += a.head;
+          if (r >= a.cap_rows) r -= a.cap_rows;
+          src = reinterpret_cast<const float4*>(a.X + r * a.ldx + j0);
+        }
+#pragma unroll
+        for (int k = 0; k < E / 4; ++k) {
+          // rows are zero padded up to ldx (a multiple of 8)
+          const float4 q = (src && j0 + 4 * k < a.ldx) ? __ldg(src + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+          xr[t][4 * k] = q.x;
+          xr[t][4 * k + 1] = q.y;
+          xr[t][4 * k + 2] = q.z;
+          xr[t][4 * k + 3] = q.w;
+        }
+      }
+    } else
     // ---- load V rows (zero padded to F) ----
     for (int idx = lane; idx < Cfg::V * Cfg::F; idx += 32) {
       const int v = idx / Cfg::F;
@@ -69,8 +103,14 @@ __global__ void __launch_bounds__(256) k_project(ProjArgs a) {
     __syncwarp();
     for (int r = 0; r < a.R; ++r) {
       const uint32_t* sw = s_signs + (size_t)r * 3 * words;
+      if constexpr (kRegRow) {
+        fwht_round_regs<L>(xr, wbuf, sw, lane);
 #pragma unroll 1
-      for (int i = 0; i < 3; ++i) fwht_round<L>(i == 0 ? xbuf : wbuf, wbuf, sw + i * words, lane);
+        for (int i = 1; i < 3; ++i) fwht_round<L>(wbuf, wbuf, sw + i * words, lane);
+      } else {
+#pragma unroll 1
+        for (int i = 0; i < 3; ++i) fwht_round<L>(i == 0 ? xbuf : wbuf, wbuf, sw + i * words, lane);
+      }
       // outputs j < D of each vector, consecutive lanes on consecutive columns
 #pragma unroll 1
       for (int vec = 0; vec < Cfg::V; ++vec) {
@@ -111,7 +151,8 @@ template <int L>
 static size_t proj_smem(int R) {
   using Cfg = FwhtCfg<L>;
   size_t sw = ((size_t)R * 3 * Cfg::words * 4 + 15) & ~(size_t)15;
-  return sw + (size_t)proj_warps<L>() * 2 * Cfg::V * Cfg::Vstride * sizeof(float);
+  const int bufs = RegRow<L>::ok ? 1 : 2;
+  return sw + (size_t)proj_warps<L>() * bufs * Cfg::V * Cfg::Vstride * sizeof(float);
 }
 
 template <int L, int MODE>
