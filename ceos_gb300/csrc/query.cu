@@ -213,9 +213,10 @@ CEOS_DEV void red_add_shared(unsigned a, float v) {
 // insertion. The capacity exceeds the number of insertions, so a free slot
 // always exists; the sequence is still bounded and returns -1 if it ran out.
 //
-// The table is two arrays, keys[cap] (int32 ids, -1 = empty) and vals[cap]
-// (float sums), so that the random key probes spread over all 32 shared-memory
-// banks. `fresh` reports that this call inserted the id.
+// In shared memory the table is two arrays, keys[cap] (int32 ids, -1 = empty)
+// and vals[cap] (float sums), so that the random key probes spread over all 32
+// banks; in global memory slot s is the pair (keys[2s], value), one sector.
+// `fresh` reports that this call inserted the id.
 template <bool SMEM>
 CEOS_DEV int table_slot(int* keys, int cap, int id, bool& fresh) {
   const uint32_t h1 = (uint32_t)id * 0x9E3779B1u;
@@ -227,12 +228,12 @@ CEOS_DEV int table_slot(int* keys, int cap, int id, bool& fresh) {
   for (int probe = 0; probe < cap; ++probe) {
     int cur;
     if (SMEM)
-      cur = ld_volatile_shared(base + 4u * (unsigned)s);
+      cur = ld_volatile_shared(base + 4u * (unsigned)s);  // shared: keys array
     else
-      cur = *reinterpret_cast<volatile int*>(&keys[s]);
+      cur = *reinterpret_cast<volatile int*>(&keys[2 * s]);  // global: (key, value) pairs
     if (cur == id) return s;
     if (cur == -1) {
-      const int prev = SMEM ? cas_shared(base + 4u * (unsigned)s, -1, id) : atomicCAS(&keys[s], -1, id);
+      const int prev = SMEM ? cas_shared(base + 4u * (unsigned)s, -1, id) : atomicCAS(&keys[2 * s], -1, id);
       if (prev == -1) {
         fresh = true;
         return s;
@@ -253,7 +254,7 @@ CEOS_DEV int table_slot(int* keys, int cap, int id, bool& fresh) {
 // an id) the add is atomic on a value initialised to -0.0f.
 template <bool SMEM>
 CEOS_DEV void table_add(float* vals, int sl, float v, bool distinct, bool fresh) {
-  float* val = vals + sl;
+  float* val = vals + (SMEM ? sl : 2 * sl);
   if (distinct) {
     *reinterpret_cast<volatile float*>(val) = fresh ? v : *reinterpret_cast<volatile float*>(val) + v;
   } else if (SMEM) {
@@ -326,9 +327,13 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_buckets(QueryArgs
   // The table pointer's address space is fixed per instantiation so that
   // shared-memory tables get shared (not generic) loads and atomics.
   const int cap_max = a.table_cap;
+  // Shared-memory tables are two arrays (keys, then values) so that random key
+  // probes spread over all banks; global tables interleave (key, value) so
+  // that a slot is one 32-byte sector. Slot i: tkeys[kS * i], tvals[kS * i].
+  constexpr int kS = SMEM_TABLE ? 1 : 2;
   int* tkeys = SMEM_TABLE ? reinterpret_cast<int*>(sm + Lq.table)
                           : reinterpret_cast<int*>(a.gtable + (long)blockIdx.x * cap_max);
-  float* tvals = reinterpret_cast<float*>(tkeys + cap_max);
+  float* tvals = SMEM_TABLE ? reinterpret_cast<float*>(tkeys + cap_max) : reinterpret_cast<float*>(tkeys) + 1;
   const int s_cap = np2(a.s > 0 ? a.s : 1);
   const int k_cap = np2(a.k > 0 ? a.k : 1);
   const unsigned long npts = (unsigned long)a.n_points;
@@ -356,8 +361,8 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_buckets(QueryArgs
       probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
     }
     for (int i = threadIdx.x; i < cap; i += blockDim.x) {
-      tkeys[i] = -1;
-      if (!a.distinct_ids) tvals[i] = -0.0f;
+      tkeys[kS * i] = -1;
+      if (!a.distinct_ids) tvals[kS * i] = -0.0f;
     }
     __syncthreads();
     // ---- 2. ordered accumulation / union of the probed bucket prefixes ----
@@ -418,8 +423,8 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_buckets(QueryArgs
       // ---- 3. top-c candidates by estimate ----
       const int nc = block_topk_hist(
           [&](long i, float& v, int& id) {
-            id = reinterpret_cast<volatile int*>(tkeys)[i];
-            v = reinterpret_cast<volatile float*>(tvals)[i];
+            id = reinterpret_cast<volatile int*>(tkeys)[kS * i];
+            v = reinterpret_cast<volatile float*>(tvals)[kS * i];
             return id >= 0;
           },
           (long)cap, a.c, cand, hist, maybe, kMaybe, scratch);
@@ -444,16 +449,16 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_buckets(QueryArgs
         const int nw = blockDim.x >> 5;
         for (int base = warp * 4; base < cap; base += nw * 4) {
           const int i = base + grp;
-          const int id = i < cap ? reinterpret_cast<volatile int*>(tkeys)[i] : -1;
+          const int id = i < cap ? reinterpret_cast<volatile int*>(tkeys)[kS * i] : -1;
           const bool active = id >= 0;
           const float d = dot_g8_bf16(qv, active ? row_ptr_bf16(a, id) : nullptr, a.ldx >> 3, g, active);
-          if (active && g == 0) tvals[i] = d;
+          if (active && g == 0) tvals[kS * i] = d;
         }
         __syncthreads();
         const int nr = block_topk_hist(
             [&](long i, float& v, int& id) {
-              id = reinterpret_cast<volatile int*>(tkeys)[i];
-              v = reinterpret_cast<volatile float*>(tvals)[i];
+              id = reinterpret_cast<volatile int*>(tkeys)[kS * i];
+              v = reinterpret_cast<volatile float*>(tvals)[kS * i];
               return id >= 0;
             },
             (long)cap, rq, resc, hist, maybe, kMaybe, scratch);
@@ -475,17 +480,17 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_buckets(QueryArgs
         const int nw = blockDim.x >> 5;
         for (int base = warp * 4; base < cap; base += nw * 4) {
           const int i = base + grp;
-          const int id = i < cap ? reinterpret_cast<volatile int*>(tkeys)[i] : -1;
+          const int id = i < cap ? reinterpret_cast<volatile int*>(tkeys)[kS * i] : -1;
           const bool active = id >= 0;
           const float d = dot_g8(qv, active ? row_ptr(a, id) : qv, a.ldx >> 2, g, active);
-          if (active && g == 0) tvals[i] = d;
+          if (active && g == 0) tvals[kS * i] = d;
         }
       }
       __syncthreads();
       nres = block_topk_hist_sorted(
           [&](long i, float& v, int& id) {
-            id = reinterpret_cast<volatile int*>(tkeys)[i];
-            v = reinterpret_cast<volatile float*>(tvals)[i];
+            id = reinterpret_cast<volatile int*>(tkeys)[kS * i];
+            v = reinterpret_cast<volatile float*>(tvals)[kS * i];
             return id >= 0;
           },
           (long)cap, kq, topk, k_cap, hist, maybe, kMaybe, scratch);
