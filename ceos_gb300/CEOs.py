@@ -19,6 +19,7 @@ ties between exactly equal values are broken towards the smaller id.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -93,6 +94,28 @@ class CEOs(_QueryAttrs):
         if h:
             self._L.ceos_destroy(h)
             self._h = None
+
+    # -- save / load (no reference counterpart) --------------------------
+    def save(self, path):
+        """Write the built index to `path` (versioned binary file with checksum)."""
+        _capi.check(self._L.ceos_save(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path):
+        """A device-resident index restored from `path`, ready to search."""
+        L = _capi.lib()
+        h = C.c_void_p()
+        _capi.check(L.ceos_load(os.fsencode(path), C.byref(h)))
+        self = cls.__new__(cls)
+        self._L, self._h = L, h
+        self._get, self._set = L.ceos_get_query_param, L.ceos_set_query_param
+        n, d = C.c_int(), C.c_int()
+        _capi.check(L.ceos_get_shape(h, C.byref(n), C.byref(d)))
+        self.n_points, self.n_features = n.value, d.value
+        p = C.c_int()
+        _capi.check(L.ceos_get_precision(h, C.byref(p)))
+        self._precision = "split_bf16" if p.value == _capi.PRECISION_SPLIT_BF16 else "fp32"
+        return self
 
     # -- parameters -----------------------------------------------------
     def setIndexParam(self, n_proj, n_repeats=1, top_m=10, n_threads=-1, random_seed=-1):
@@ -289,6 +312,28 @@ class streamCEOs(_QueryAttrs):
         X = _rows(X, self.n_features, "new_dataset")
         ptr = X.ctypes.data if X.shape[0] else None
         _capi.check(self._L.ceos_stream_update(self._h, C.c_void_p(ptr), X.shape[0], int(n_delPoints)))
+
+    def save(self, path):
+        """Write the built stream index to `path` (versioned binary file with checksum)."""
+        _capi.check(self._L.ceos_stream_save(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path):
+        """A device-resident stream index restored from `path`."""
+        L = _capi.lib()
+        h = C.c_void_p()
+        _capi.check(L.ceos_stream_load(os.fsencode(path), C.byref(h)))
+        self = cls.__new__(cls)
+        self._L, self._h = L, h
+        self._get, self._set = L.ceos_stream_get_query_param, L.ceos_stream_set_query_param
+        v = [C.c_int() for _ in range(5)]
+        _capi.check(L.ceos_stream_get_index_param(h, *[C.byref(x) for x in v]))
+        self._D, self._R, self._m = v[0].value, v[1].value, v[2].value
+        self.n_features = v[4].value
+        p = C.c_int()
+        _capi.check(L.ceos_stream_get_precision(h, C.byref(p)))
+        self._precision = "split_bf16" if p.value == _capi.PRECISION_SPLIT_BF16 else "fp32"
+        return self
 
     def set_reserve(self, reserve: int):
         """Exact maintenance (no reference counterpart): with reserve >= 0, set before

@@ -107,6 +107,14 @@ SIGNATURES = {
     "ceos_stream_delete": (C.c_int, [VP, VP, C.c_int]),
     "ceos_bruteforce_fp64": (C.c_int, [F32P, C.c_long, C.c_int, F32P, C.c_int, C.c_int, I32P,
                                        np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")]),
+    "ceos_get_shape": (C.c_int, [VP, IP, IP]),
+    "ceos_get_precision": (C.c_int, [VP, IP]),
+    "ceos_stream_get_index_param": (C.c_int, [VP, IP, IP, IP, IP, IP]),
+    "ceos_stream_get_precision": (C.c_int, [VP, IP]),
+    "ceos_save": (C.c_int, [VP, C.c_char_p]),
+    "ceos_load": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
+    "ceos_stream_save": (C.c_int, [VP, C.c_char_p]),
+    "ceos_stream_load": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
     "ceos_server_config_init": (C.c_int, [C.POINTER(ServerConfig)]),
     "ceos_server_create": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),
     "ceos_server_create_stream": (C.c_int, [VP, C.POINTER(ServerConfig), C.POINTER(VP)]),

@@ -210,6 +210,24 @@ int ceos_stream_delete(ceos_stream* h, const int32_t* ids, int n_ids);
 int ceos_stream_size(const ceos_stream* h, int* n_points);
 int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals);
 
+/* ---- save / load (no reference counterpart: the reference rebuilds every index) ----
+ * A versioned binary file (magic "CEOSGB3", version 1) with the parameters, the rows in
+ * logical order, the sign words and the built structures (buckets, or the dense CEOs-Est
+ * projections; for streams with a reserve also the per-list counts and thresholds), closed by
+ * an FNV-1a checksum. A loaded index is device resident and searches / updates exactly like
+ * the saved one without rebuilding. Loading a file of the other kind, another version, or a
+ * truncated or corrupt file fails with CEOS_ERR_ARG. */
+/* Shape, precision and stream parameters of a handle (e.g. after a load). */
+int ceos_get_shape(const ceos_index* h, int* n_points, int* n_features);
+int ceos_get_precision(const ceos_index* h, int* precision);
+int ceos_stream_get_index_param(const ceos_stream* h, int* n_proj, int* n_repeats,
+                                int* top_points, int* seed, int* n_features);
+int ceos_stream_get_precision(const ceos_stream* h, int* precision);
+int ceos_save(const ceos_index* h, const char* path);
+int ceos_load(const char* path, ceos_index** out);
+int ceos_stream_save(const ceos_stream* h, const char* path);
+int ceos_stream_load(const char* path, ceos_stream** out);
+
 /* ---- ground truth (no reference counterpart in the library) -------------
  * Exact top-k maximum inner products of Q (nq x d) against X (n x d), row-major host
  * float32, computed on the GPU in FP64 (float products are exact in double; double

@@ -347,3 +347,27 @@ def test_bruteforce_fp64_matches_oracle(gpu, oracle, n, d, k, kind):
     oi, os_ = oracle.bruteforce(X, Q, k)
     assert np.array_equal(gi, oi)
     assert np.array_equal(gs.view(np.uint64), os_.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_config0_full_size_parity(gpu, oracle):
+    """The CPU-runnable configuration at full size: 17,770 x 300 rows g*s
+    (g ~ N(0, I/300), s ~ LogNormal(0, 0.5)), 1000 N(0, I) queries, n_proj 1024,
+    n_repeats 2, top_m 100, n_probed_vectors 20, n_cand 500, k 10, seed 42:
+    buckets and search results bit-exact against the oracle, and recall@10
+    against the FP64 ground truth."""
+    from ceos_gb300 import _capi
+
+    X = netflix_like(17770, 300, seed=0)
+    Q = gaussian_queries(1000, 300, seed=1)
+    g, o = build_pair(gpu, oracle, X, 1024, 2, 100, 42, kind="coceos")
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+    for idx in (g, o):
+        idx.n_probed_vectors, idx.n_cand = 20, 500
+    a = g.search_coCEOs_Est(Q, 10)
+    b = o.search_coCEOs_Est(Q, 10)
+    assert np.array_equal(a[0], b[0]) and bits_equal(a[1], b[1])
+    gt, _ = _capi.bruteforce_fp64(X, Q, 10)
+    assert recall(a[0], gt) > 0.3
