@@ -95,6 +95,13 @@ class CEOs(_QueryAttrs):
             self._L.ceos_destroy(h)
             self._h = None
 
+    def build_from_file(self, path, algo="coceos"):
+        """Build from a raw row-major float32 file of n_points x n_features values (the
+        reference's loadbinData format, src/Utilities.cpp:142-214), streamed to the GPU.
+        algo: "dense" (build), "coceos" (build_coCEOs_Est) or "hash" (build_CEOs_Hash)."""
+        code = {"dense": _capi.ALGO_DENSE, "coceos": _capi.ALGO_COCEOS, "hash": _capi.ALGO_HASH}[algo]
+        _capi.check(self._L.ceos_build_from_file(self._h, os.fsencode(path), code))
+
     # -- save / load (no reference counterpart) --------------------------
     def save(self, path):
         """Write the built index to `path` (versioned binary file with checksum)."""
@@ -312,6 +319,10 @@ class streamCEOs(_QueryAttrs):
         X = _rows(X, self.n_features, "new_dataset")
         ptr = X.ctypes.data if X.shape[0] else None
         _capi.check(self._L.ceos_stream_update(self._h, C.c_void_p(ptr), X.shape[0], int(n_delPoints)))
+
+    def build_from_file(self, path, n_points):
+        """build() from the first n_points rows of a raw row-major float32 file."""
+        _capi.check(self._L.ceos_stream_build_from_file(self._h, os.fsencode(path), int(n_points)))
 
     def save(self, path):
         """Write the built stream index to `path` (versioned binary file with checksum)."""

@@ -111,6 +111,8 @@ SIGNATURES = {
     "ceos_get_precision": (C.c_int, [VP, IP]),
     "ceos_stream_get_index_param": (C.c_int, [VP, IP, IP, IP, IP, IP]),
     "ceos_stream_get_precision": (C.c_int, [VP, IP]),
+    "ceos_build_from_file": (C.c_int, [VP, C.c_char_p, C.c_int]),
+    "ceos_stream_build_from_file": (C.c_int, [VP, C.c_char_p, C.c_int]),
     "ceos_save": (C.c_int, [VP, C.c_char_p]),
     "ceos_load": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
     "ceos_stream_save": (C.c_int, [VP, C.c_char_p]),

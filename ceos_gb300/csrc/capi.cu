@@ -123,8 +123,11 @@ int ceos_set_precision(ceos_index* h, int precision) {
   return CEOS_OK;
 }
 
+// Rows of a build come from host memory, or from a file when `path` is set.
+static thread_local const char* g_build_path = nullptr;
+
 static int index_build_common(ceos_index* h, const float* X, const char* what) {
-  if (!h || !X) return fail(CEOS_ERR_ARG, "null argument");
+  if (!h || (!X && !g_build_path)) return fail(CEOS_ERR_ARG, "null argument");
   if (h->core.attached) return fail(CEOS_ERR_BUSY, "the index is owned by a server");
   Core& c = h->core;
   ST_TRY(c.check_param());
@@ -135,7 +138,10 @@ static int index_build_common(ceos_index* h, const float* X, const char* what) {
   c.head = 0;
   c.cap_rows = h->n_points;
   CUDA_TRY(c.dX.ensure((size_t)c.n_rows * c.ldx * 4));
-  ST_TRY(c.upload_rows(X, c.n_rows, c.dX.as<float>()));
+  if (g_build_path)
+    ST_TRY(c.upload_rows_from_file(g_build_path, c.n_rows, c.dX.as<float>()));
+  else
+    ST_TRY(c.upload_rows(X, c.n_rows, c.dX.as<float>()));
   ST_TRY(c.upload_signs());
   c.proj_tensor = (c.precision == CEOS_PRECISION_SPLIT_BF16 && project_tc_supported(c.L)) ? 1 : 0;
   c.timer.mark("h2d");
@@ -145,6 +151,8 @@ static int index_build_common(ceos_index* h, const float* X, const char* what) {
   }
   return CEOS_OK;
 }
+
+static int ceos_build_coceos_est_or_hash(ceos_index* h, int algo);
 
 int ceos_build(ceos_index* h, const float* X) {
   ST_TRY(index_build_common(h, X, "Building CEOs index..."));
@@ -164,9 +172,46 @@ int ceos_build(ceos_index* h, const float* X) {
   return CEOS_OK;
 }
 
+// CEOs-Hash centering (opt-in `centering`): the reference subtracts the
+// n-vector of row means from every d-dimensional row (src/CEOs.cpp:721-728,
+// `matX.rowwise().mean()`), which does not type-check as a column centering.
+// Here the rows are centered by the d-vector of column means, computed in a
+// fixed order (double sums per chunk of kCenterChunk rows, chunks added in
+// order, mean rounded to float), before the projection; the rerank then uses
+// the centered rows, as the reference's does, so reported scores are
+// q . (x - mean). Queries are not centered.
+constexpr long kCenterChunk = 4096;
+
+static int center_rows(Core& c) {
+  const long n = c.n_rows;
+  const int d = c.n_features;
+  const long chunks = (n + kCenterChunk - 1) / kCenterChunk;
+  DevBuf part, mu;
+  CUDA_TRY(part.ensure((size_t)chunks * d * 8));
+  CUDA_TRY(launch_col_partial_sums(c.dX.as<float>(), n, d, c.ldx, kCenterChunk, part.as<double>(), c.stream));
+  std::vector<double> hp((size_t)chunks * d);
+  CUDA_TRY(cudaMemcpyAsync(hp.data(), part.p, hp.size() * 8, cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(cudaStreamSynchronize(c.stream));
+  std::vector<float> hm(d);
+  for (int j = 0; j < d; ++j) {
+    double s = 0.0;
+    for (long b = 0; b < chunks; ++b) s += hp[(size_t)b * d + j];
+    hm[j] = (float)(s / (double)n);
+  }
+  CUDA_TRY(mu.ensure((size_t)d * 4));
+  CUDA_TRY(cudaMemcpyAsync(mu.p, hm.data(), (size_t)d * 4, cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(launch_center_rows(c.dX.as<float>(), n, d, c.ldx, mu.as<float>(), c.stream));
+  CUDA_TRY(cudaStreamSynchronize(c.stream));
+  return CEOS_OK;
+}
+
 static int build_buckets_api(ceos_index* h, const float* X, int kind, const char* what) {
   ST_TRY(index_build_common(h, X, what));
   Core& c = h->core;
+  if (kind == B_HASH && c.centering) {
+    ST_TRY(center_rows(c));
+    c.timer.mark("centering");
+  }
   const int st = c.build_buckets();
   if (st != CEOS_OK) {
     c.timer.clear();
@@ -180,12 +225,29 @@ static int build_buckets_api(ceos_index* h, const float* X, int kind, const char
   return CEOS_OK;
 }
 
+static int ceos_build_coceos_est_or_hash(ceos_index* h, int algo) {
+  return algo == CEOS_ALGO_COCEOS
+             ? build_buckets_api(h, nullptr, B_COCEOS, "Building coCEOs-Estimate index...")
+             : build_buckets_api(h, nullptr, B_HASH, "Building CEOs-Hash index...");
+}
+
 int ceos_build_coceos_est(ceos_index* h, const float* X) {
   return build_buckets_api(h, X, B_COCEOS, "Building coCEOs-Estimate index...");
 }
 
 int ceos_build_ceos_hash(ceos_index* h, const float* X) {
   return build_buckets_api(h, X, B_HASH, "Building CEOs-Hash index...");
+}
+
+int ceos_build_from_file(ceos_index* h, const char* path, int algo) {
+  if (!path) return fail(CEOS_ERR_ARG, "null path");
+  if (algo != CEOS_ALGO_DENSE && algo != CEOS_ALGO_COCEOS && algo != CEOS_ALGO_HASH)
+    return fail(CEOS_ERR_ARG, "unknown algo %d", algo);
+  g_build_path = path;
+  const int st = algo == CEOS_ALGO_DENSE ? ceos_build(h, nullptr)
+                                         : ceos_build_coceos_est_or_hash(h, algo);
+  g_build_path = nullptr;
+  return st;
 }
 
 // Reference validation order: n_probed_points first, then n_probed_vectors
@@ -392,7 +454,7 @@ int ceos_stream_get_query_param(const ceos_stream* h, int* s, int* p, int* c) {
 }
 
 int ceos_stream_build(ceos_stream* h, const float* X, int n_points) {
-  if (!h || !X) return fail(CEOS_ERR_ARG, "null argument");
+  if (!h || (!X && !g_build_path)) return fail(CEOS_ERR_ARG, "null argument");
   if (h->core.attached) return fail(CEOS_ERR_BUSY, "the index is owned by a server");
   if (n_points < 1) return fail(CEOS_ERR_ARG, "n_points must be >= 1");
   Core& c = h->core;
@@ -404,7 +466,10 @@ int ceos_stream_build(ceos_stream* h, const float* X, int n_points) {
   c.head = 0;
   c.cap_rows = n_points;
   CUDA_TRY(c.dX.ensure((size_t)c.cap_rows * c.ldx * 4));
-  ST_TRY(c.upload_rows(X, c.n_rows, c.dX.as<float>()));
+  if (g_build_path)
+    ST_TRY(c.upload_rows_from_file(g_build_path, c.n_rows, c.dX.as<float>()));
+  else
+    ST_TRY(c.upload_rows(X, c.n_rows, c.dX.as<float>()));
   ST_TRY(c.upload_signs());
   c.proj_tensor = (c.precision == CEOS_PRECISION_SPLIT_BF16 && project_tc_supported(c.L)) ? 1 : 0;
   c.timer.mark("h2d");
@@ -580,6 +645,14 @@ int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals) {
   CUDA_TRY(cudaMemcpy2D(ids, w, c.dBids.p, ld, w, rows, cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemcpy2D(vals, w, c.dBvals.p, ld, w, rows, cudaMemcpyDeviceToHost));
   return CEOS_OK;
+}
+
+int ceos_stream_build_from_file(ceos_stream* h, const char* path, int n_points) {
+  if (!path) return fail(CEOS_ERR_ARG, "null path");
+  g_build_path = path;
+  const int st = ceos_stream_build(h, nullptr, n_points);
+  g_build_path = nullptr;
+  return st;
 }
 
 int ceos_stream_set_reserve(ceos_stream* h, int reserve) {

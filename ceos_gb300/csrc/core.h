@@ -303,6 +303,12 @@ struct Core {
     return CEOS_OK;
   }
 
+  // Rows n x n_features from a raw row-major float32 file (the reference's
+  // loadbinData format, src/Utilities.cpp:142-214) into dst (n x ldx), streamed
+  // through mmap and two pinned chunks, so the file never has to fit in host
+  // memory at once. Defined in ingest.cu.
+  int upload_rows_from_file(const char* path, long n, float* dst);
+
   ProjArgs proj_base() const {
     ProjArgs a;
     a.X = dX.as<float>();

@@ -129,6 +129,12 @@ cudaError_t launch_stream_delete(int C, int M, int m, const int* del, int nd, in
 cudaError_t launch_compact_rows(const float* X, long head, long cap, long n, int ldx,
                                 const int* del, int nd, float* dst, cudaStream_t st);
 
+// ---- CEOs-Hash centering (stream.cu) ----
+// per-chunk column sums in double, rows [b*chunk, (b+1)*chunk) summed in order
+cudaError_t launch_col_partial_sums(const float* X, long n, int d, int ldx, long chunk, double* partial,
+                                    cudaStream_t st);
+cudaError_t launch_center_rows(float* X, long n, int d, int ldx, const float* mu, cudaStream_t st);
+
 // ---- misc ----
 cudaError_t launch_pad_rows(const float* src, long n, int d, float* dst, int ldx, cudaStream_t st);
 // bfloat16 copy (round to nearest even) of n rows of stride ldx

@@ -254,6 +254,44 @@ cudaError_t launch_compact_rows(const float* X, long head, long cap, long n, int
   return cudaGetLastError();
 }
 
+// Column means for CEOs-Hash centering, in a fixed order: block b sums rows
+// [b * chunk, (b + 1) * chunk) of every column sequentially in double; the
+// host adds the per-chunk sums in chunk order.
+__global__ void k_col_partial_sums(const float* X, long n, int d, int ldx, long chunk, double* partial) {
+  const long r0 = (long)blockIdx.x * chunk;
+  const long r1 = min(n, r0 + chunk);
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    double s = 0.0;
+    for (long r = r0; r < r1; ++r) s += (double)X[r * ldx + j];
+    partial[(long)blockIdx.x * d + j] = s;
+  }
+}
+
+cudaError_t launch_col_partial_sums(const float* X, long n, int d, int ldx, long chunk, double* partial,
+                                    cudaStream_t st) {
+  const long blocks = (n + chunk - 1) / chunk;
+  if (blocks <= 0) return cudaSuccess;
+  k_col_partial_sums<<<(unsigned)blocks, 128, 0, st>>>(X, n, d, ldx, chunk, partial);
+  return cudaGetLastError();
+}
+
+__global__ void k_center_rows(float* X, long n, int d, int ldx, const float* mu) {
+  const long total = n * (long)d;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long r = i / d;
+    const int j = (int)(i % d);
+    X[r * ldx + j] -= mu[j];
+  }
+}
+
+cudaError_t launch_center_rows(float* X, long n, int d, int ldx, const float* mu, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  long blocks = (n * d + 255) / 256;
+  if (blocks > 8192) blocks = 8192;
+  k_center_rows<<<(unsigned)blocks, 256, 0, st>>>(X, n, d, ldx, mu);
+  return cudaGetLastError();
+}
+
 // Copy rows into a zero-padded row stride (ldx >= d, multiple of 4).
 __global__ void k_pad_rows(const float* src, long n, int d, float* dst, int ldx) {
   const long total = n * (long)ldx;

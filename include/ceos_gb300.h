@@ -210,6 +210,17 @@ int ceos_stream_delete(ceos_stream* h, const int32_t* ids, int n_ids);
 int ceos_stream_size(const ceos_stream* h, int* n_points);
 int ceos_stream_get_buckets(const ceos_stream* h, int32_t* ids, float* vals);
 
+/* ---- file ingestion ------------------------------------------------------
+ * Build from a raw row-major float32 file holding at least n_points x n_features values: the
+ * format the reference's loadbinData reads (src/Utilities.cpp:142-214), where the file is
+ * mmapped and copied into an in-memory matrix before the build. Here the mapped rows stream
+ * to the device through two pinned chunks, so the file never has to fit in host memory.
+ * algo: CEOS_ALGO_DENSE (build), CEOS_ALGO_COCEOS (build_coCEOs_Est), CEOS_ALGO_HASH
+ * (build_CEOs_Hash). A file with fewer rows fails with CEOS_ERR_ARG (the reference exits,
+ * src/Utilities.cpp:171-175). */
+int ceos_build_from_file(ceos_index* h, const char* path, int algo);
+int ceos_stream_build_from_file(ceos_stream* h, const char* path, int n_points);
+
 /* ---- save / load (no reference counterpart: the reference rebuilds every index) ----
  * A versioned binary file (magic "CEOSGB3", version 1) with the parameters, the rows in
  * logical order, the sign words and the built structures (buckets, or the dense CEOs-Est

@@ -416,11 +416,33 @@ struct OracleCEOs {
     return ST_OK;
   }
 
+  // CEOs-Hash centering as the GPU library defines it (the reference's
+  // src/CEOs.cpp:721-728 subtracts the n-vector of row means from every row,
+  // which is not a column centering): column means as double sums over
+  // chunks of 4096 rows, chunks added in order, rounded to float; each row
+  // minus the means. The stored rows, used by the rerank, are the centered ones.
+  void center_rows() {
+    const long n = n_points, chunk = 4096, chunks = (n + chunk - 1) / chunk;
+    std::vector<float> mu(n_features);
+    for (int j = 0; j < n_features; ++j) {
+      double total = 0.0;
+      for (long b = 0; b < chunks; ++b) {
+        double sb = 0.0;
+        for (long r = b * chunk; r < std::min(n, (b + 1) * chunk); ++r) sb += (double)X[(size_t)r * n_features + j];
+        total += sb;
+      }
+      mu[j] = (float)(total / (double)n);
+    }
+    for (long r = 0; r < n; ++r)
+      for (int j = 0; j < n_features; ++j) X[(size_t)r * n_features + j] -= mu[j];
+  }
+
   // src/CEOs.cpp:311-441 (with_vals) and :708-840 (ids only)
   int build_buckets(const float* Xin, bool with_vals) {
     omp_set_num_threads(n_threads);
     if (top_m < 1 || top_m > n_points) return ST_BAD_ARG;
     common_build(Xin);
+    if (!with_vals && centering) center_rows();
     const int Cc = C();
     std::vector<float> Pt((size_t)n_points * Cc);
     project_rows(X.data(), n_points, n_features, fhtDim, n_proj, n_repeats, bits.data(), Pt.data());
@@ -906,6 +928,7 @@ float orc_dot(const float* q, const float* x, int d) { return dot_fma(q, x, d); 
 int orc_ceos_build_dense(void* h, const float* X) { return ((OracleCEOs*)h)->build_dense(X); }
 int orc_ceos_build_coceos(void* h, const float* X) { return ((OracleCEOs*)h)->build_buckets(X, true); }
 int orc_ceos_build_hash(void* h, const float* X) { return ((OracleCEOs*)h)->build_buckets(X, false); }
+void orc_ceos_set_centering(void* h, int c) { ((OracleCEOs*)h)->centering = c != 0; }
 int orc_ceos_search_dense(void* h, const float* Q, int nq, int k, int* ids, float* d) {
   return ((OracleCEOs*)h)->search_dense(Q, nq, k, ids, d);
 }

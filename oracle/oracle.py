@@ -118,6 +118,8 @@ def lib():
             L.orc_stream_estimate_search.argtypes = [vp, _F32P, C.c_int, C.c_int, _I32P, _F32P]
             L.orc_stream_hash_search.argtypes = [vp, _F32P, C.c_int, C.c_int, _I32P, _F32P]
             L.orc_stream_get_buckets.argtypes = [vp, _I32P, _F32P]
+            L.orc_ceos_set_centering.argtypes = [vp, C.c_int]
+            L.orc_ceos_set_centering.restype = None
             L.orc_stream_set_exact.argtypes = [vp, C.c_int]
             L.orc_stream_set_exact.restype = None
             L.orc_stream_delete.argtypes = [vp, _I32P, C.c_int]
@@ -264,10 +266,19 @@ class CEOs(_Attrs):
         self._get_q = L.orc_ceos_get_query
         self._set_q = L.orc_ceos_set_query
         self.n_points, self.n_features = int(n_points), int(n_features)
-        self.centering = False
+        self._centering = False
         self._D = 256
         self._R = 1
         self._m = 100
+
+    @property
+    def centering(self):
+        return self._centering
+
+    @centering.setter
+    def centering(self, v):
+        self._centering = bool(v)
+        self._L.orc_ceos_set_centering(self._h, 1 if v else 0)
 
     def __del__(self):
         h = getattr(self, "_h", None)

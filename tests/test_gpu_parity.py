@@ -371,3 +371,32 @@ def test_config0_full_size_parity(gpu, oracle):
     assert np.array_equal(a[0], b[0]) and bits_equal(a[1], b[1])
     gt, _ = _capi.bruteforce_fp64(X, Q, 10)
     assert recall(a[0], gt) > 0.3
+
+
+@pytest.mark.gpu
+def test_hash_centering_matches_oracle(gpu, oracle):
+    """Opt-in CEOs-Hash centering by the column means (the reference's branch,
+    src/CEOs.cpp:721-728, subtracts an n-vector of row means from d-vectors):
+    buckets and search bit-exact against the oracle, scores are q . (x - mean),
+    and the index differs from the uncentered one on nonnegative data."""
+    n, d = 9000, 64
+    X = sift_like(n, d, seed=77)
+    Q = sift_like(30, d, seed=78)
+    g, o = gpu.CEOs(n, d), oracle.CEOs(n, d)
+    for idx in (g, o):
+        idx.setIndexParam(128, 2, 50, 4, 21)
+        idx.centering = True
+        idx.build_CEOs_Hash(X)
+        idx.n_probed_vectors, idx.n_probed_points = 20, 30
+    gi, _ = g.buckets()
+    oi, _ = o.buckets()
+    assert np.array_equal(gi, oi)
+    a, b = g.search_CEOs_Hash(Q, 10), o.search_CEOs_Hash(Q, 10)
+    assert np.array_equal(a[0], b[0]) and bits_equal(a[1], b[1])
+    mu = X.astype(np.float64).mean(axis=0)
+    want = np.einsum("qkd,qd->qk", X[a[0]].astype(np.float64) - mu, Q.astype(np.float64))
+    np.testing.assert_allclose(a[1], want, rtol=1e-4, atol=1e-2)
+    u = gpu.CEOs(n, d)
+    u.setIndexParam(128, 2, 50, 4, 21)
+    u.build_CEOs_Hash(X)
+    assert not np.array_equal(u.buckets()[0], gi)

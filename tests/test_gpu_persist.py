@@ -76,3 +76,34 @@ def test_save_unbuilt_and_missing(gpu, tmp_path):
         g.save(str(tmp_path / "x.ceos"))
     with pytest.raises(ValueError):
         gpu.CEOs.load(str(tmp_path / "missing.ceos"))
+
+
+@pytest.mark.parametrize("kind", ["coceos", "hash", "dense"])
+def test_build_from_file_equals_build(gpu, tmp_path, kind):
+    """Rows streamed from a raw float32 file (the reference's loadbinData format,
+    here 21 rows more than n_points and d = 50, not a multiple of 8) give the
+    same index as the in-memory build."""
+    n, d = 7000, 50
+    X = netflix_like(n + 21, d, seed=12)
+    path = tmp_path / "rows.bin"
+    X.tofile(str(path))
+    Q = gaussian_queries(25, d, seed=13)
+    a, b = gpu.CEOs(n, d), gpu.CEOs(n, d)
+    for g in (a, b):
+        g.setIndexParam(64, 2, 40, 8, 3)
+        g.n_probed_vectors, g.n_probed_points, g.n_cand = 10, 30, 200
+    {"coceos": a.build_coCEOs_Est, "hash": a.build_CEOs_Hash, "dense": a.build}[kind](X[:n])
+    b.build_from_file(str(path), kind)
+    search = {"coceos": "search_coCEOs_Est", "hash": "search_CEOs_Hash", "dense": "search"}[kind]
+    ra, rb = getattr(a, search)(Q, 10), getattr(b, search)(Q, 10)
+    assert np.array_equal(ra[0], rb[0]) and np.array_equal(ra[1], rb[1])
+    big = gpu.CEOs(n + 22, d)
+    big.setIndexParam(64, 2, 40, 8, 3)
+    with pytest.raises(ValueError, match="exceeds"):
+        big.build_from_file(str(path), kind)
+    s, t = gpu.streamCEOs(d), gpu.streamCEOs(d)
+    for x in (s, t):
+        x.setIndexParam(64, 2, 40, 8, 3)
+    s.build(X[:n])
+    t.build_from_file(str(path), n)
+    assert np.array_equal(s.buckets()[0], t.buckets()[0])
