@@ -195,7 +195,7 @@ struct Core {
   DevBuf dX, dSigns, dP, dBids, dBvals;
   DevBuf dXb;  // bfloat16 copy of the rows (split precision), same ring layout
   bool xb_valid = false;
-  DevBuf wStage, wQ, wQproj, wIds, wD, wTable, wProbes, wEst, wNewP, wNewX;
+  DevBuf wStage, wQ, wQproj, wIds, wD, wTable, wProbes, wEst, wNewP, wNewX, wSort;
   Timer timer;
   int attached = 0;  // a serving loop owns the index (serve.cu)
   // streamCEOs maintenance: -1 = the reference's (FIFO update refilled from
@@ -251,7 +251,7 @@ struct Core {
 
   void release_all() {
     DevBuf* bufs[] = {&dX, &dSigns, &dP, &dBids, &dBvals, &dXb, &wStage, &wQ, &wQproj, &wIds,
-                      &wD, &wTable, &wProbes, &wEst, &wNewP, &wNewX, &dCnt, &dTau};
+                      &wD, &wTable, &wProbes, &wEst, &wNewP, &wNewX, &wSort, &dCnt, &dTau};
     xb_valid = false;
     for (DevBuf* b : bufs) b->release();
     built = B_NONE;
@@ -511,6 +511,7 @@ struct Core {
   // coCEOs-Est / CEOs-Hash / stream searches over the buckets.
   int search_buckets(int mode, const float* Q, long nq, int k, int32_t* ids, float* dists,
                      bool on_device, cudaStream_t user_stream) {
+    (void)user_stream;
     ST_TRY(ensure_bf16());
     timer.begin(stream);
     ST_TRY(stage_queries(Q, nq, on_device));
@@ -525,6 +526,15 @@ struct Core {
     }
     q.out_ids = out_ids;
     q.out_d = out_d;
+    if (mode == Q_ESTIMATE && use_sorted()) {
+      ST_TRY(sorted_args(q, nq));
+      const size_t ssm = query_sorted_smem(q);
+      const int grid = (int)std::min<long>(nq, (long)sms * std::max(query_sorted_blocks_per_sm(ssm), 1));
+      CUDA_TRY(wSort.ensure((size_t)std::max(grid, 1) * 2 * q.sort_cap * 8));
+      q.sort_scratch = wSort.as<int2>();
+      CUDA_TRY(launch_query_sorted(q, std::max(grid, 1), ssm, stream));
+      return finish_search(mode, nq, k, ids, dists, out_ids, out_d, on_device);
+    }
     const long tc = table_capacity(s, p);
     if (tc < 0) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
     q.table_cap = (int)tc;
@@ -545,6 +555,31 @@ struct Core {
       q.gtable = wTable.as<uint64_t>();
     }
     CUDA_TRY(launch_query_buckets(q, mode, std::max(grid, 1), smem, stream));
+    return finish_search(mode, nq, k, ids, dists, out_ids, out_d, on_device);
+  }
+
+  // Sort-based estimate accumulation (k_query_sorted): on unless the
+  // environment sets CEOS_GB300_QUERY=table.
+  static bool use_sorted() {
+    const char* e = std::getenv("CEOS_GB300_QUERY");
+    return !(e && std::strcmp(e, "table") == 0);
+  }
+
+  int sorted_args(QueryArgs& q, long nq) const {
+    (void)nq;
+    const long pairs = (long)std::max(s, 0) * std::max(p, 0);
+    if (pairs > INT_MAX / 2) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
+    q.sort_cap = std::max(pairs, 1L);
+    int bits = 1;
+    while (bits < 31 && (1L << bits) <= n_rows) ++bits;
+    q.id_bits = bits;  // ids 0 .. n_rows (n_rows marks dropped entries)
+    if (query_sorted_smem(q) > smem_optin)
+      return fail(CEOS_ERR_UNSUPPORTED, "query working set (n_cand=%d, n_neighbors=%d) exceeds shared memory", c, q.k);
+    return CEOS_OK;
+  }
+
+  int finish_search(int mode, long nq, int k, int32_t* ids, float* dists, int32_t* out_ids,
+                    float* out_d, bool on_device) {
     timer.mark(mode == Q_ESTIMATE ? "estimate+rerank" : "union+rerank");
     if (!on_device) {
       CUDA_TRY(cudaMemcpyAsync(ids, out_ids, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, stream));
@@ -553,7 +588,6 @@ struct Core {
     }
     CUDA_TRY(cudaStreamSynchronize(stream));
     timer.finish();
-    (void)user_stream;
     return CEOS_OK;
   }
 

@@ -95,13 +95,21 @@ struct QueryArgs {
   const int* probes = nullptr;  // [nq][s] tags in pop order
   float* est = nullptr;         // [nq][n]
   int* probes_out = nullptr;
-  uint64_t* gkeys = nullptr;    // [grid][...] rerank workspace (hash union)
-  int gkeys_cap = 0;
+  // sort-based estimate accumulation (k_query_sorted): per-CTA scratch of
+  // 2 x sort_cap (id, value) pairs, ids below 2^id_bits
+  int2* sort_scratch = nullptr;
+  long sort_cap = 0;
+  int id_bits = 0;
 };
 
 enum QueryMode { Q_ESTIMATE = 0, Q_UNION = 1 };
 
 cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem, cudaStream_t st);
+// Sort-based coCEOs-Est search (distinct ids per column): stable radix sort of the
+// probed (id, value) pairs by id, in-order run sums, top-c, rerank, top-k.
+cudaError_t launch_query_sorted(const QueryArgs& a, int grid, size_t smem, cudaStream_t st);
+size_t query_sorted_smem(const QueryArgs& a);
+int query_sorted_blocks_per_sm(size_t smem);
 size_t query_buckets_smem(const QueryArgs& a, int mode);
 int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem);
 cudaError_t launch_probe_select(const QueryArgs& a, cudaStream_t st);

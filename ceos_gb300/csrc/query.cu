@@ -565,6 +565,291 @@ int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem) {
 }
 
 // ---------------------------------------------------------------------------
+// Sort-based coCEOs-Est accumulation.
+//
+// The estimate of an id is the sum of its values over the probed columns in
+// probe order (src/CEOs.cpp:562-610). Instead of a hash table, the CTA
+// gathers the s x p probed (id, value) pairs in probe order into a per-CTA
+// scratch, sorts them by id with a stable LSD radix sort (8-bit digits, one
+// contiguous segment per warp, warp-private digit offsets, lanes ranked by a
+// match), and sums each run of equal ids in order: the stable sort keeps a
+// run in probe order, so the sums are the reference's (first value as is,
+// then added term by term). Entries whose id is not a live point (stale
+// streamCEOs rows) are mapped to id n_points and dropped. The run sums form a
+// compact candidate list for the top-c; rerank and top-k are as in
+// k_query_buckets.
+
+constexpr int kRadixBins = 256;
+constexpr int kSortWarps = kQueryThreads / 32;
+
+struct SLayout {
+  size_t qv, pkeys, probes, topk, resc, cand, hist, maybe, rhist, total;
+};
+
+__host__ __device__ inline SLayout s_layout(const QueryArgs& a) {
+  SLayout L;
+  size_t o = 0;
+  L.qv = o;
+  o = al16(o + (size_t)a.ldx * 4);
+  L.pkeys = o;
+  o = al16(o + (size_t)np2(a.s > 0 ? a.s : 1) * 8);
+  L.probes = o;
+  o = al16(o + (size_t)(a.s > 0 ? a.s : 1) * 4);
+  L.topk = o;
+  o = al16(o + (size_t)np2(a.k > 0 ? a.k : 1) * 8);
+  L.resc = o;
+  o = al16(o + (size_t)(a.rescore > 0 ? a.rescore : 0) * 8);
+  L.cand = o;
+  o = al16(o + (size_t)(a.c > 0 ? a.c : 1) * 8);
+  L.hist = o;
+  o = al16(o + (size_t)kHistBins * 4);
+  L.maybe = o;
+  o = al16(o + (size_t)kMaybe * 8);
+  // the radix digit tables are live only during the sort, when cand / hist /
+  // maybe are not: they share that space
+  L.rhist = L.cand;
+  const size_t rend = al16(L.rhist + (size_t)2 * kSortWarps * kRadixBins * 4);
+  L.total = o > rend ? o : rend;
+  return L;
+}
+
+size_t query_sorted_smem(const QueryArgs& a) { return s_layout(a).total; }
+
+template <int MINB>
+__global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ uint32_t scratch[16];
+  __shared__ int wsum[kQueryThreads / 32];
+  const SLayout Lq = s_layout(a);
+  float* qv = reinterpret_cast<float*>(sm + Lq.qv);
+  uint64_t* pkeys = reinterpret_cast<uint64_t*>(sm + Lq.pkeys);
+  int* probes = reinterpret_cast<int*>(sm + Lq.probes);
+  uint64_t* topk = reinterpret_cast<uint64_t*>(sm + Lq.topk);
+  uint64_t* resc = reinterpret_cast<uint64_t*>(sm + Lq.resc);
+  uint64_t* cand = reinterpret_cast<uint64_t*>(sm + Lq.cand);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(sm + Lq.hist);
+  uint64_t* maybe = reinterpret_cast<uint64_t*>(sm + Lq.maybe);
+  // digit counts per warp segment: [2][kSortWarps][kRadixBins], the current
+  // pass's table and the next pass's, filled while this pass scatters
+  int* rh_all = reinterpret_cast<int*>(sm + Lq.rhist);
+  const int s_cap = np2(a.s > 0 ? a.s : 1);
+  const int k_cap = np2(a.k > 0 ? a.k : 1);
+  const int npts = (int)a.n_points;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int2* bufA = a.sort_scratch + (long)blockIdx.x * 2 * a.sort_cap;
+  int2* bufB = bufA + a.sort_cap;
+
+  const int nq = a.d_nq ? min(*a.d_nq, a.nq) : a.nq;
+  for (int q = blockIdx.x; q < nq; q += gridDim.x) {
+    const int sq = a.q_s ? min(a.q_s[q], a.s) : a.s;
+    const int kq = a.q_k ? min(a.q_k[q], a.k) : a.k;
+    const long oq = a.q_off ? a.q_off[q] : (long)q * a.k;
+    const int rq = (a.q_k && a.rescore_per_k > 0) ? min(a.rescore, a.rescore_per_k * kq) : a.rescore;
+    for (int j = threadIdx.x; j < a.ldx; j += blockDim.x) qv[j] = a.Q[(long)q * a.ldx + j];
+    // ---- 1. probes: top-s |projection|, consumed worst first ----
+    const float* qp = a.qproj + (long)q * a.C;
+    const int ns = block_topk_hist_sorted(
+        [&](long i, float& v, int& id) {
+          v = abs_ref(qp[i]);
+          id = (int)i;
+          return true;
+        },
+        (long)a.C, sq, pkeys, s_cap, hist, maybe, kMaybe, scratch);
+    for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+      const int col = key_id(pkeys[ns - 1 - j]);
+      probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
+    }
+    __syncthreads();
+    // ---- 2. gather the probed pairs in probe order ----
+    const int E = ns * a.p;
+    constexpr int kU = 8;  // independent loads in flight per thread in every pass
+    const int seg = (E + kSortWarps - 1) / kSortWarps;
+    for (int i = threadIdx.x; i < 2 * kSortWarps * kRadixBins; i += blockDim.x) rh_all[i] = 0;
+    __syncthreads();
+    for (int t0 = threadIdx.x; t0 < E; t0 += kU * blockDim.x) {
+      int id[kU];
+      float v[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int t = t0 + u * blockDim.x;
+        id[u] = npts;
+        v[u] = 0.0f;
+        if (t < E) {
+          const int j = t / a.p, e = t - j * a.p;
+          const int tag = probes[j];
+          const int col = (tag < 0 ? -tag : tag) - 1;
+          const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m + e;
+          id[u] = __ldg(a.bids + base);
+          v[u] = __ldg(a.bvals + base);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int t = t0 + u * blockDim.x;
+        if (t < E) {
+          const int i = (unsigned)id[u] >= (unsigned)npts ? npts : id[u];  // stale row: dropped below
+          bufA[t] = make_int2(i, __float_as_int(v[u]));
+          atomicAdd(&rh_all[(t / seg) * kRadixBins + (i & 255)], 1);  // first pass's digit counts
+        }
+      }
+    }
+    __syncthreads();
+    // ---- 3. stable LSD radix sort by id ----
+    int2* src = bufA;
+    int2* dst = bufB;
+    const int w0 = min(E, warp * seg), w1 = min(E, w0 + seg);
+    int cur = 0;
+    for (int shift = 0; shift < a.id_bits; shift += 8, cur ^= 1) {
+      int* rh = rh_all + cur * kSortWarps * kRadixBins;
+      int* rn = rh_all + (cur ^ 1) * kSortWarps * kRadixBins;
+      int* myh = rh + warp * kRadixBins;
+      const bool more = shift + 8 < a.id_bits;
+      // digit d: exclusive offset over digits, then over warps within the digit
+      int tot = 0;
+      if (threadIdx.x < kRadixBins)
+        for (int w = 0; w < kSortWarps; ++w) tot += rh[w * kRadixBins + threadIdx.x];
+      int inc = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+      }
+      if (threadIdx.x < kRadixBins && lane == 31) wsum[warp] = inc;
+      __syncthreads();
+      if (threadIdx.x < kRadixBins) {
+        int off = inc - tot;
+        for (int w = 0; w < warp; ++w) off += wsum[w];
+        for (int w = 0; w < kSortWarps; ++w) {
+          const int c = rh[w * kRadixBins + threadIdx.x];
+          rh[w * kRadixBins + threadIdx.x] = off;
+          off += c;
+        }
+      }
+      __syncthreads();
+      for (int c0 = w0; c0 < w1; c0 += 32 * kU) {
+        int2 v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = c0 + 32 * u + lane;
+          v[u] = i < w1 ? src[i] : make_int2(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const bool has = c0 + 32 * u + lane < w1;
+          const int dg = has ? ((v[u].x >> shift) & 255) : 0;
+          // lanes with the same digit: one ballot per digit bit
+          unsigned peers = __ballot_sync(0xffffffffu, has);
+#pragma unroll
+          for (int bit = 0; bit < 8; ++bit) {
+            const unsigned bb = __ballot_sync(0xffffffffu, (dg >> bit) & 1);
+            peers &= ((dg >> bit) & 1) ? bb : ~bb;
+          }
+          const int rank = __popc(peers & ((1u << lane) - 1u));
+          const int b = has ? myh[dg] : 0;
+          __syncwarp();
+          if (has) {
+            dst[b + rank] = v[u];
+            if (rank == 0) myh[dg] = b + __popc(peers);
+            // the next pass's digit counts, by destination segment
+            if (more) atomicAdd(&rn[((b + rank) / seg) * kRadixBins + ((v[u].x >> (shift + 8)) & 255)], 1);
+          }
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < kSortWarps * kRadixBins; i += blockDim.x) rh[i] = 0;  // next-next pass
+      int2* t = src;
+      src = dst;
+      dst = t;
+    }
+    // ---- 4. in-order run sums -> compact (value, id) list in dst ----
+    if (threadIdx.x == 0) scratch[8] = 0u;
+    __syncthreads();
+    // each warp takes 32 consecutive elements per step; the previous id comes
+    // from the neighbour lane, so a step needs one load per lane (and a run
+    // that continues past the step is walked by its head lane)
+    for (int c0 = warp * 32 * kU; c0 < E; c0 += kSortWarps * 32 * kU) {
+      int2 v[kU];
+      int prev0 = -1;
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int i = c0 + 32 * u + lane;
+        v[u] = i < E ? src[i] : make_int2(-1, 0);
+      }
+      if (lane == 0 && c0 > 0) prev0 = src[c0 - 1].x;
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int i = c0 + 32 * u + lane;
+        int prev = __shfl_up_sync(0xffffffffu, v[u].x, 1);
+        const int last = __shfl_sync(0xffffffffu, v[u > 0 ? u - 1 : 0].x, 31);
+        if (lane == 0) prev = u == 0 ? prev0 : last;
+        const int id = v[u].x;
+        const bool head = i < E && id < npts && id != prev;
+        float sum = 0.0f;
+        if (head) {
+          sum = __int_as_float(v[u].y);
+          for (int j = i + 1; j < E; ++j) {
+            const int2 w = src[j];
+            if (w.x != id) break;
+            sum = sum + __int_as_float(w.y);
+          }
+        }
+        const uint32_t pos = warp_reserve(head, &scratch[8]);
+        if (head) dst[pos] = make_int2(id, __float_as_int(sum));
+      }
+    }
+    __syncthreads();
+    const int U = (int)scratch[8];
+    __syncthreads();
+    // ---- 5. top-c by estimate, rerank, top-k ----
+    const int nc = block_topk_hist(
+        [&](long i, float& v, int& id) {
+          const int2 w = dst[i];
+          id = w.x;
+          v = __int_as_float(w.y);
+          return true;
+        },
+        (long)U, a.c, cand, hist, maybe, kMaybe, scratch);
+    const int ns2 = score_candidates(a, rq, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
+    const int nres = block_topk_hist_sorted(
+        [&](long i, float& v, int& id) {
+          const uint64_t k = cand[i];
+          v = key_val(k);
+          id = key_id(k);
+          return true;
+        },
+        (long)ns2, kq, topk, k_cap, hist, maybe, kMaybe, scratch);
+    for (int i = threadIdx.x; i < kq; i += blockDim.x) {
+      a.out_ids[oq + i] = i < nres ? key_id(topk[i]) : 0;
+      a.out_d[oq + i] = i < nres ? key_val(topk[i]) : 0.0f;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_query_sorted(const QueryArgs& a, int grid, size_t smem, cudaStream_t st) {
+  if (a.nq <= 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_query_sorted<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  k_query_sorted<2><<<grid, kQueryThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+int query_sorted_blocks_per_sm(size_t smem) {
+  int n = 0;
+  cudaError_t e = cudaFuncSetAttribute(k_query_sorted<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_sorted<2>, kQueryThreads, smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n;
+}
+
+// ---------------------------------------------------------------------------
 // Dense CEOs-Est.
 
 __global__ void __launch_bounds__(256) k_probe_select(QueryArgs a) {
