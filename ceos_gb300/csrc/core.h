@@ -526,7 +526,7 @@ struct Core {
     }
     q.out_ids = out_ids;
     q.out_d = out_d;
-    if (mode == Q_ESTIMATE && use_sorted()) {
+    if (mode == Q_ESTIMATE && use_sorted(q)) {
       ST_TRY(sorted_args(q, nq));
       const size_t ssm = query_sorted_smem(q);
       const int grid = (int)std::min<long>(nq, (long)sms * std::max(query_sorted_blocks_per_sm(ssm), 1));
@@ -558,11 +558,18 @@ struct Core {
     return finish_search(mode, nq, k, ids, dists, out_ids, out_d, on_device);
   }
 
-  // Sort-based estimate accumulation (k_query_sorted): on unless the
-  // environment sets CEOS_GB300_QUERY=table.
-  static bool use_sorted() {
+  // Estimate searches run sorted (k_query_sorted) unless the hash table fits
+  // in shared memory with two CTAs per SM; CEOS_GB300_QUERY=table|sorted
+  // forces one form.
+  bool use_sorted(const QueryArgs& q) const {
     const char* e = std::getenv("CEOS_GB300_QUERY");
-    return !(e && std::strcmp(e, "table") == 0);
+    if (e && std::strcmp(e, "table") == 0) return false;
+    if (e && std::strcmp(e, "sorted") == 0) return true;
+    const long tc = table_capacity(q.s, q.p);
+    if (tc < 0) return true;
+    QueryArgs t = q;
+    t.table_cap = (int)tc;
+    return !query_table_preferred(t);
   }
 
   int sorted_args(QueryArgs& q, long nq) const {

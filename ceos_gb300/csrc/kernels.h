@@ -110,6 +110,9 @@ cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t 
 cudaError_t launch_query_sorted(const QueryArgs& a, int grid, size_t smem, cudaStream_t st);
 size_t query_sorted_smem(const QueryArgs& a);
 int query_sorted_blocks_per_sm(size_t smem);
+// true when the estimate search is faster with its hash table in shared memory
+// (two CTAs per SM) than sorted; a.table_cap must be set
+bool query_table_preferred(const QueryArgs& a);
 size_t query_buckets_smem(const QueryArgs& a, int mode);
 int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem);
 cudaError_t launch_probe_select(const QueryArgs& a, cudaStream_t st);

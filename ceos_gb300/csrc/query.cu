@@ -836,6 +836,13 @@ cudaError_t launch_query_sorted(const QueryArgs& a, int grid, size_t smem, cudaS
   return cudaGetLastError();
 }
 
+bool query_table_preferred(const QueryArgs& a) {
+  // the shared-memory table wins while two 512-thread CTAs fit per SM
+  QueryArgs t = a;
+  t.table_in_smem = 1;
+  return two_per_sm(q_layout(t, Q_ESTIMATE).total);
+}
+
 int query_sorted_blocks_per_sm(size_t smem) {
   int n = 0;
   cudaError_t e = cudaFuncSetAttribute(k_query_sorted<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

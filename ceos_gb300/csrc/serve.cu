@@ -92,7 +92,7 @@ struct MetaLayout {
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
-  DevBuf dStage, dQ, dQproj, dMeta, dIds, dD, dTable;
+  DevBuf dStage, dQ, dQproj, dMeta, dIds, dD, dTable, dSort;
   Pinned<float> hQ;
   Pinned<unsigned char> hMeta;
   Pinned<int32_t> hIds;
@@ -113,6 +113,8 @@ struct ceos_server {
   int d = 0, ldx = 0, C = 0, p = 0, c = 0;
   int max_cap = 0;
   bool table_in_smem = true;
+  bool sorted = false;  // estimate searches through k_query_sorted
+  long sort_cap = 0;
   size_t smem = 0;
   int grid_max = 1;
   size_t slot_bytes = 0;
@@ -178,6 +180,13 @@ struct ceos_server {
     q.table_cap = max_cap;
     q.table_in_smem = table_in_smem ? 1 : 0;
     q.gtable = table_in_smem ? nullptr : sl.dTable.as<uint64_t>();
+    if (sorted) {
+      q.sort_scratch = sl.dSort.as<int2>();
+      q.sort_cap = sort_cap;
+      int bits = 1;
+      while (bits < 31 && (1L << bits) <= core->n_rows) ++bits;
+      q.id_bits = bits;  // from the current size: graphs are captured again after updates
+    }
     return q;
   }
 
@@ -201,7 +210,10 @@ struct ceos_server {
     CUDA_TRY(launch_project(a, PROJ_ROWS, core->L, core->sms, st));
     QueryArgs q = slot_args(sl, rows);
     const int grid = std::max(1, std::min(rows, grid_max));
-    CUDA_TRY(launch_query_buckets(q, mode, grid, smem, st));
+    if (sorted)
+      CUDA_TRY(launch_query_sorted(q, grid, smem, st));
+    else
+      CUDA_TRY(launch_query_buckets(q, mode, grid, smem, st));
     const size_t outb = (size_t)rows * cfg.max_neighbors * 4;
     CUDA_TRY(cudaMemcpyAsync(sl.hIds.p, sl.dIds.p, outb, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(sl.hD.p, sl.dD.p, outb, cudaMemcpyDeviceToHost, st));
@@ -463,13 +475,28 @@ int server_create(Core& c, ceos_stream* sh, const ceos_server_config* cfg_in, ce
   }
   S.table_in_smem = q.table_in_smem != 0;
   S.smem = smem;
-  const int per_sm = std::max(1, query_buckets_blocks_per_sm(mode, smem, S.table_in_smem));
+  int per_sm = std::max(1, query_buckets_blocks_per_sm(mode, smem, S.table_in_smem));
+  if (mode == Q_ESTIMATE && c.use_sorted(q)) {
+    // the sorted estimate path, for the largest requests
+    S.sorted = true;
+    S.sort_cap = std::max(1L, (long)cfg.max_probed_vectors * c.p);
+    QueryArgs qs = q;
+    qs.sort_cap = S.sort_cap;
+    S.smem = query_sorted_smem(qs);
+    if (S.smem > c.smem_optin)
+      return fail(CEOS_ERR_UNSUPPORTED, "query working set (n_cand=%d, max_neighbors=%d) exceeds shared memory",
+                  c.c, cfg.max_neighbors);
+    S.table_in_smem = true;
+    per_sm = std::max(1, query_sorted_blocks_per_sm(S.smem));
+  }
   S.grid_max = std::max(1, std::min(cfg.max_batch, c.sms * per_sm));
   // device bytes of one slot
   const size_t B = (size_t)cfg.max_batch;
   const size_t stage = S.ldx == S.d ? 0 : B * S.d * 4;
   const size_t table = S.table_in_smem ? 0 : (size_t)S.grid_max * S.max_cap * 8;
-  S.slot_bytes = stage + B * S.ldx * 4 + B * S.C * 4 + S.meta.bytes + 2 * B * cfg.max_neighbors * 4 + table;
+  const size_t sortb = S.sorted ? (size_t)S.grid_max * 2 * S.sort_cap * 8 : 0;
+  S.slot_bytes = stage + B * S.ldx * 4 + B * S.C * 4 + S.meta.bytes + 2 * B * cfg.max_neighbors * 4 + table +
+                 sortb;
   int n_slots = cfg.n_slots;
   if (cfg.mem_budget_bytes > 0)
     n_slots = (int)std::min<long long>(n_slots, cfg.mem_budget_bytes / (long long)S.slot_bytes);
@@ -488,6 +515,7 @@ int server_create(Core& c, ceos_stream* sh, const ceos_server_config* cfg_in, ce
     CUDA_TRY(sl->dIds.ensure(B * cfg.max_neighbors * 4));
     CUDA_TRY(sl->dD.ensure(B * cfg.max_neighbors * 4));
     if (table) CUDA_TRY(sl->dTable.ensure(table));
+    if (sortb) CUDA_TRY(sl->dSort.ensure(sortb));
     CUDA_TRY(sl->hQ.alloc(B * S.d));
     std::memset(sl->hQ.p, 0, B * S.d * 4);
     CUDA_TRY(sl->hMeta.alloc(S.meta.bytes));
