@@ -98,19 +98,28 @@ CEOS_DEV float dot_g8_bf16(const float* __restrict__ q, const uint16_t* __restri
   const uint4* x8 = reinterpret_cast<const uint4*>(x);
   const float4* q4 = reinterpret_cast<const float4*>(q);
   float s = 0.0f;
+  auto acc8 = [&](const uint4 w, int c) {
+    const float4 qa = q4[2 * c], qb = q4[2 * c + 1];
+    s = __fmaf_rn(qa.x, __uint_as_float(w.x << 16), s);
+    s = __fmaf_rn(qa.y, __uint_as_float(w.x & 0xffff0000u), s);
+    s = __fmaf_rn(qa.z, __uint_as_float(w.y << 16), s);
+    s = __fmaf_rn(qa.w, __uint_as_float(w.y & 0xffff0000u), s);
+    s = __fmaf_rn(qb.x, __uint_as_float(w.z << 16), s);
+    s = __fmaf_rn(qb.y, __uint_as_float(w.z & 0xffff0000u), s);
+    s = __fmaf_rn(qb.z, __uint_as_float(w.w << 16), s);
+    s = __fmaf_rn(qb.w, __uint_as_float(w.w & 0xffff0000u), s);
+  };
   if (active) {
-    for (int c = g; c < n8; c += 8) {
-      const uint4 w = __ldcg(x8 + c);
-      const float4 qa = q4[2 * c], qb = q4[2 * c + 1];
-      s = __fmaf_rn(qa.x, __uint_as_float(w.x << 16), s);
-      s = __fmaf_rn(qa.y, __uint_as_float(w.x & 0xffff0000u), s);
-      s = __fmaf_rn(qa.z, __uint_as_float(w.y << 16), s);
-      s = __fmaf_rn(qa.w, __uint_as_float(w.y & 0xffff0000u), s);
-      s = __fmaf_rn(qb.x, __uint_as_float(w.z << 16), s);
-      s = __fmaf_rn(qb.y, __uint_as_float(w.z & 0xffff0000u), s);
-      s = __fmaf_rn(qb.z, __uint_as_float(w.w << 16), s);
-      s = __fmaf_rn(qb.w, __uint_as_float(w.w & 0xffff0000u), s);
+    int c = g;
+    // four loads in flight, then the FMAs in chunk order
+    for (; c + 24 < n8; c += 32) {
+      uint4 w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) w[u] = __ldcg(x8 + c + 8 * u);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc8(w[u], c + 8 * u);
     }
+    for (; c < n8; c += 8) acc8(__ldcg(x8 + c), c);
   }
   s = s + __shfl_xor_sync(0xffffffffu, s, 4);
   s = s + __shfl_xor_sync(0xffffffffu, s, 2);
