@@ -794,13 +794,26 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
         if (lane == 0) prev = u == 0 ? prev0 : last;
         const int id = v[u].x;
         const bool head = i < E && id < npts && id != prev;
-        float sum = 0.0f;
+        float sum = head ? __int_as_float(v[u].y) : 0.0f;
+        // add the run's following values in order: first from the next lanes
+        // (shuffles), then, for a run that reaches the end of these 32, from memory
         if (head) {
-          sum = __int_as_float(v[u].y);
-          for (int j = i + 1; j < E; ++j) {
-            const int2 w = src[j];
-            if (w.x != id) break;
-            sum = sum + __int_as_float(w.y);
+          // the run's following values, in order; four pairs per round trip
+          int j = i + 1;
+          bool go = true;
+          while (go && j < E) {
+            int2 w[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) w[t] = j + t < E ? src[j + t] : make_int2(-1, 0);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              if (go && w[t].x == id) {
+                sum = sum + __int_as_float(w[t].y);
+              } else {
+                go = false;
+              }
+            }
+            j += 4;
           }
         }
         const uint32_t pos = warp_reserve(head, &scratch[8]);
