@@ -669,7 +669,7 @@ def main():
             "build_s": build_s, "build_phases_ms": build_phases,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_query_buckets<estimate>",
+                         "kernel": "k_query_sorted (coCEOs-Est, sorted accumulation)",
                          "bytes_per_query": bytes_per_query, "kernel_ms": kern_s * 1e3},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": Q.nbytes,
