@@ -219,20 +219,23 @@ CEOS_DEV uint32_t warp_reserve(bool want, uint32_t* counter) {
   return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// pre (optional): min key, max key and count of the valid items, already
+// known to the caller; pass 1 is then skipped.
 template <typename GetItem>
 __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32_t* hist,
-                               uint64_t* maybe, int maybe_cap, uint32_t* scratch) {
+                               uint64_t* maybe, int maybe_cap, uint32_t* scratch,
+                               const uint32_t* pre = nullptr) {
   const int lane = threadIdx.x & 31;
   // ---- pass 1: min / max keys and count ----
   if (threadIdx.x == 0) {
-    scratch[0] = 0xffffffffu;  // min key
-    scratch[1] = 0u;           // max key
-    scratch[2] = 0u;           // valid count
-    scratch[3] = 0u;           // out count
-    scratch[4] = 0u;           // maybe count
+    scratch[0] = pre ? pre[0] : 0xffffffffu;  // min key
+    scratch[1] = pre ? pre[1] : 0u;           // max key
+    scratch[2] = pre ? pre[2] : 0u;           // valid count
+    scratch[3] = 0u;                          // out count
+    scratch[4] = 0u;                          // maybe count
   }
   __syncthreads();
-  {
+  if (!pre) {
     uint32_t lo = 0xffffffffu, hi = 0u, cnt = 0u;
     for (long i = threadIdx.x; i < N; i += blockDim.x) {
       float v;

@@ -772,8 +772,13 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       dst = t;
     }
     // ---- 4. in-order run sums -> compact (value, id) list in dst ----
-    if (threadIdx.x == 0) scratch[8] = 0u;
+    if (threadIdx.x == 0) {
+      scratch[8] = 0u;
+      scratch[9] = 0xffffffffu;  // min key of the sums
+      scratch[10] = 0u;          // max key
+    }
     __syncthreads();
+    uint32_t klo = 0xffffffffu, khi = 0u;
     // each warp takes 32 consecutive elements per step; the previous id comes
     // from the neighbour lane, so a step needs one load per lane (and a run
     // that continues past the step is walked by its head lane)
@@ -817,11 +822,25 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
           }
         }
         const uint32_t pos = warp_reserve(head, &scratch[8]);
-        if (head) dst[pos] = make_int2(id, __float_as_int(sum));
+        if (head) {
+          dst[pos] = make_int2(id, __float_as_int(sum));
+          klo = min(klo, fkey(sum));
+          khi = max(khi, fkey(sum));
+        }
       }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      klo = min(klo, __shfl_xor_sync(0xffffffffu, klo, o));
+      khi = max(khi, __shfl_xor_sync(0xffffffffu, khi, o));
+    }
+    if (lane == 0) {
+      atomicMin(&scratch[9], klo);
+      atomicMax(&scratch[10], khi);
     }
     __syncthreads();
     const int U = (int)scratch[8];
+    const uint32_t pre[3] = {scratch[9], scratch[10], (uint32_t)U};
     __syncthreads();
     // ---- 5. top-c by estimate, rerank, top-k ----
     const int nc = block_topk_hist(
@@ -831,7 +850,7 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
           v = __int_as_float(w.y);
           return true;
         },
-        (long)U, a.c, cand, hist, maybe, kMaybe, scratch);
+        (long)U, a.c, cand, hist, maybe, kMaybe, scratch, pre);
     const int ns2 = score_candidates(a, rq, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
     const int nres = block_topk_hist_sorted(
         [&](long i, float& v, int& id) {
