@@ -206,6 +206,9 @@ __device__ int block_topk_sorted(GetKey get, long N, int K, uint64_t* out, int c
 // scratch = 16 u32. All threads of the block must call it; blockDim.x must be
 // a multiple of 32.
 constexpr int kHistBins = 2048;
+// items loaded per thread before they are used, in the histogram and
+// compaction passes (the items usually come from L2 or HBM)
+constexpr int kTopkU = 2;
 
 CEOS_DEV uint32_t warp_reserve(bool want, uint32_t* counter) {
   const unsigned m = __ballot_sync(0xffffffffu, want);
@@ -237,14 +240,25 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   __syncthreads();
   if (!pre) {
     uint32_t lo = 0xffffffffu, hi = 0u, cnt = 0u;
-    for (long i = threadIdx.x; i < N; i += blockDim.x) {
-      float v;
-      int id;
-      if (get(i, v, id)) {
-        const uint32_t k = fkey(v);
-        lo = min(lo, k);
-        hi = max(hi, k);
-        ++cnt;
+    for (long base = 0; base < N; base += kTopkU * blockDim.x) {
+      float v[kTopkU];
+      int id[kTopkU];
+      bool ok[kTopkU];
+#pragma unroll
+      for (int u = 0; u < kTopkU; ++u) {
+        const long i = base + u * blockDim.x + threadIdx.x;
+        v[u] = 0.f;
+        id[u] = 0;
+        ok[u] = i < N && get(i, v[u], id[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kTopkU; ++u) {
+        if (ok[u]) {
+          const uint32_t k = fkey(v[u]);
+          lo = min(lo, k);
+          hi = max(hi, k);
+          ++cnt;
+        }
       }
     }
 #pragma unroll
@@ -304,12 +318,20 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   // ---- pass 2: histogram ----
   for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) hist[b] = 0;
   __syncthreads();
-  for (long base = 0; base < N; base += blockDim.x) {
-    const long i = base + threadIdx.x;
-    float v = 0.f;
-    int id = 0;
-    const bool ok = i < N && get(i, v, id);
-    if (ok) atomicAdd(&hist[bin_of(v)], 1u);
+  for (long base = 0; base < N; base += kTopkU * blockDim.x) {
+    float v[kTopkU];
+    int id[kTopkU];
+    bool ok[kTopkU];
+#pragma unroll
+    for (int u = 0; u < kTopkU; ++u) {
+      const long i = base + u * blockDim.x + threadIdx.x;
+      v[u] = 0.f;
+      id[u] = 0;
+      ok[u] = i < N && get(i, v[u], id[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kTopkU; ++u)
+      if (ok[u]) atomicAdd(&hist[bin_of(v[u])], 1u);
   }
   __syncthreads();
   // ---- threshold bin: block-wide suffix scan over the bins ----
@@ -351,18 +373,27 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   const uint32_t need = (uint32_t)K - above;
   const bool fits = inbin <= (uint32_t)maybe_cap;
   // ---- pass 3: compaction ----
-  for (long base = 0; base < N; base += blockDim.x) {
-    const long i = base + threadIdx.x;
-    float v = 0.f;
-    int id = 0;
-    const bool ok = i < N && get(i, v, id);
-    const int b = ok ? bin_of(v) : -1;
-    const bool sure = ok && b > tb;
-    const bool cand = ok && b == tb && fits;
-    const uint32_t p1 = warp_reserve(sure, &scratch[3]);
-    if (sure) out[p1] = pack_key(v, id);
-    const uint32_t p2 = warp_reserve(cand, &scratch[4]);
-    if (cand) maybe[p2] = pack_key(v, id);
+  for (long base = 0; base < N; base += kTopkU * blockDim.x) {
+    float v[kTopkU];
+    int id[kTopkU];
+    bool ok[kTopkU];
+#pragma unroll
+    for (int u = 0; u < kTopkU; ++u) {
+      const long i = base + u * blockDim.x + threadIdx.x;
+      v[u] = 0.f;
+      id[u] = 0;
+      ok[u] = i < N && get(i, v[u], id[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kTopkU; ++u) {
+      const int b = ok[u] ? bin_of(v[u]) : -1;
+      const bool sure = ok[u] && b > tb;
+      const bool cand = ok[u] && b == tb && fits;
+      const uint32_t p1 = warp_reserve(sure, &scratch[3]);
+      if (sure) out[p1] = pack_key(v[u], id[u]);
+      const uint32_t p2 = warp_reserve(cand, &scratch[4]);
+      if (cand) maybe[p2] = pack_key(v[u], id[u]);
+    }
   }
   __syncthreads();
   if (fits) {
