@@ -579,17 +579,40 @@ int query_buckets_blocks_per_sm(int mode, size_t smem, bool table_in_smem) {
 // The estimate of an id is the sum of its values over the probed columns in
 // probe order (src/CEOs.cpp:562-610). Instead of a hash table, the CTA
 // gathers the s x p probed (id, value) pairs in probe order into a per-CTA
-// scratch, sorts them by id with a stable LSD radix sort (8-bit digits, one
-// contiguous segment per warp, warp-private digit offsets, lanes ranked by a
-// match), and sums each run of equal ids in order: the stable sort keeps a
-// run in probe order, so the sums are the reference's (first value as is,
-// then added term by term). Entries whose id is not a live point (stale
-// streamCEOs rows) are mapped to id n_points and dropped. The run sums form a
-// compact candidate list for the top-c; rerank and top-k are as in
-// k_query_buckets.
+// scratch and brings equal ids together with stable scatters (one contiguous
+// segment per warp, warp-private digit offsets, lanes ranked by ballots), so
+// that the pairs of one id stay in probe order and their sums are the
+// reference's (first value as is, then added term by term):
+//   * ids below 2^20 (partitioned accumulation): ONE stable scatter by
+//     id >> 10 into at most 1024 partitions of 1024 ids. Each warp then
+//     walks the partitions of its share (a contiguous run of the scattered
+//     pairs) 32 pairs at a time, summing into a shared-memory table of 1024
+//     floats indexed by id & 1023; a one-byte tag per slot names the
+//     partition whose id the slot holds. Lanes that hit the same slot are
+//     applied by the lowest of them in lane order (a match per 32 pairs);
+//     when a pair of a later partition reaches a slot, the slot's finished
+//     sum is written out first, and the remaining slots are written out at
+//     the end;
+//   * larger ids: a stable LSD radix sort (8-bit digits) and in-order sums
+//     over each run of equal ids.
+// Entries whose id is not a live point (stale streamCEOs rows) are mapped to
+// id n_points and dropped. The sums form a compact candidate list for the
+// top-c; rerank and top-k are as in k_query_buckets.
 
 constexpr int kRadixBins = 256;
 constexpr int kSortWarps = kQueryThreads / 32;
+constexpr int kPartTableBits = 10;                // ids per accumulation table
+constexpr int kPartTable = 1 << kPartTableBits;
+constexpr int kPartMaxBits = 10;                  // partitions: at most 1024
+constexpr int kPartIdBits = kPartTableBits + kPartMaxBits;
+// shared-memory region of the sort phase (aliases cand / hist / maybe)
+constexpr size_t kPartCountsBytes = (size_t)kSortWarps * (1 << kPartMaxBits) * 4;  // digit counts
+constexpr size_t kPartTablesBytes = (size_t)kSortWarps * kPartTable * 4;           // alias the counts
+constexpr size_t kPartTagOff = kPartCountsBytes > kPartTablesBytes ? kPartCountsBytes : kPartTablesBytes;
+constexpr size_t kPartStageOff = kPartTagOff + (size_t)kSortWarps * kPartTable;    // one byte per slot
+constexpr size_t kPartStartOff = kPartStageOff + (size_t)kSortWarps * 32 * 8;
+constexpr size_t kPartRegion = kPartStartOff + (((size_t)(1 << kPartMaxBits) + 1) * 4 + 15) / 16 * 16;
+constexpr size_t kLsdRegion = (size_t)2 * kSortWarps * kRadixBins * 4;
 
 struct SLayout {
   size_t qv, pkeys, probes, topk, resc, cand, hist, maybe, rhist, total;
@@ -614,10 +637,12 @@ __host__ __device__ inline SLayout s_layout(const QueryArgs& a) {
   o = al16(o + (size_t)kHistBins * 4);
   L.maybe = o;
   o = al16(o + (size_t)kMaybe * 8);
-  // the radix digit tables are live only during the sort, when cand / hist /
-  // maybe are not: they share that space
+  // the digit tables, partition starts and accumulation tables are live only
+  // during the sort and the sums, when cand / hist / maybe are not: they
+  // share that space (sized for either path, so that a launch configured for
+  // one index size stays valid as a stream index grows)
   L.rhist = L.cand;
-  const size_t rend = al16(L.rhist + (size_t)2 * kSortWarps * kRadixBins * 4);
+  const size_t rend = al16(L.rhist + (kPartRegion > kLsdRegion ? kPartRegion : kLsdRegion));
   L.total = o > rend ? o : rend;
   return L;
 }
@@ -629,6 +654,7 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ uint32_t scratch[16];
   __shared__ int wsum[kQueryThreads / 32];
+  __shared__ int wcnt[kQueryThreads / 32];
   const SLayout Lq = s_layout(a);
   float* qv = reinterpret_cast<float*>(sm + Lq.qv);
   uint64_t* pkeys = reinterpret_cast<uint64_t*>(sm + Lq.pkeys);
@@ -673,7 +699,14 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     const int E = ns * a.p;
     constexpr int kU = 8;  // independent loads in flight per thread in every pass
     const int seg = (E + kSortWarps - 1) / kSortWarps;
-    for (int i = threadIdx.x; i < 2 * kSortWarps * kRadixBins; i += blockDim.x) rh_all[i] = 0;
+    // partitioned accumulation: digit = id >> tb (hb bits); else 8-bit LSD digits
+    const bool part = a.id_bits <= kPartIdBits;
+    const int tb = min(a.id_bits, kPartTableBits);
+    const int hb = part ? a.id_bits - tb : 8;
+    const int nbins = 1 << hb;
+    const int dshift0 = part ? tb : 0;
+    for (int i = threadIdx.x; i < (part ? kSortWarps * nbins : 2 * kSortWarps * kRadixBins); i += blockDim.x)
+      rh_all[i] = 0;
     __syncthreads();
     for (int t0 = threadIdx.x; t0 < E; t0 += kU * blockDim.x) {
       int id[kU];
@@ -698,41 +731,54 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
         if (t < E) {
           const int i = (unsigned)id[u] >= (unsigned)npts ? npts : id[u];  // stale row: dropped below
           bufA[t] = make_int2(i, __float_as_int(v[u]));
-          atomicAdd(&rh_all[(t / seg) * kRadixBins + (i & 255)], 1);  // first pass's digit counts
+          atomicAdd(&rh_all[(t / seg) * nbins + ((i >> dshift0) & (nbins - 1))], 1);  // first pass's digits
         }
       }
     }
     __syncthreads();
-    // ---- 3. stable LSD radix sort by id ----
+    // ---- 3. stable scatter(s) by id digits ----
     int2* src = bufA;
     int2* dst = bufB;
     const int w0 = min(E, warp * seg), w1 = min(E, w0 + seg);
+    int* pstart = reinterpret_cast<int*>(sm + Lq.rhist + kPartStartOff);
+    const int npass = part ? 1 : (a.id_bits + 7) / 8;
     int cur = 0;
-    for (int shift = 0; shift < a.id_bits; shift += 8, cur ^= 1) {
-      int* rh = rh_all + cur * kSortWarps * kRadixBins;
+    for (int ps = 0; ps < npass; ++ps, cur ^= 1) {
+      const int shift = part ? tb : 8 * ps;
+      int* rh = rh_all + (part ? 0 : cur * kSortWarps * kRadixBins);
       int* rn = rh_all + (cur ^ 1) * kSortWarps * kRadixBins;
-      int* myh = rh + warp * kRadixBins;
-      const bool more = shift + 8 < a.id_bits;
-      // digit d: exclusive offset over digits, then over warps within the digit
+      int* myh = rh + warp * nbins;
+      const bool more = !part && shift + 8 < a.id_bits;
+      // digit d: exclusive offset over digits, then over warps within the
+      // digit; thread t owns digits [t*dper, (t+1)*dper)
+      const int dper = (nbins + kQueryThreads - 1) / kQueryThreads;
+      const int d0 = threadIdx.x * dper;
       int tot = 0;
-      if (threadIdx.x < kRadixBins)
-        for (int w = 0; w < kSortWarps; ++w) tot += rh[w * kRadixBins + threadIdx.x];
+      for (int j = 0; j < dper; ++j)
+        if (d0 + j < nbins)
+          for (int w = 0; w < kSortWarps; ++w) tot += rh[w * nbins + d0 + j];
       int inc = tot;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int v = __shfl_up_sync(0xffffffffu, inc, o);
         if (lane >= o) inc += v;
       }
-      if (threadIdx.x < kRadixBins && lane == 31) wsum[warp] = inc;
+      if (lane == 31) wsum[warp] = inc;
       __syncthreads();
-      if (threadIdx.x < kRadixBins) {
+      {
         int off = inc - tot;
         for (int w = 0; w < warp; ++w) off += wsum[w];
-        for (int w = 0; w < kSortWarps; ++w) {
-          const int c = rh[w * kRadixBins + threadIdx.x];
-          rh[w * kRadixBins + threadIdx.x] = off;
-          off += c;
+        for (int j = 0; j < dper; ++j) {
+          const int d = d0 + j;
+          if (d >= nbins) break;
+          if (part) pstart[d] = off;
+          for (int w = 0; w < kSortWarps; ++w) {
+            const int c = rh[w * nbins + d];
+            rh[w * nbins + d] = off;
+            off += c;
+          }
         }
+        if (part && threadIdx.x == 0) pstart[nbins] = E;
       }
       __syncthreads();
       for (int c0 = w0; c0 < w1; c0 += 32 * kU) {
@@ -745,13 +791,15 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
           const bool has = c0 + 32 * u + lane < w1;
-          const int dg = has ? ((v[u].x >> shift) & 255) : 0;
+          const int dg = has ? ((v[u].x >> shift) & (nbins - 1)) : 0;
           // lanes with the same digit: one ballot per digit bit
           unsigned peers = __ballot_sync(0xffffffffu, has);
 #pragma unroll
-          for (int bit = 0; bit < 8; ++bit) {
-            const unsigned bb = __ballot_sync(0xffffffffu, (dg >> bit) & 1);
-            peers &= ((dg >> bit) & 1) ? bb : ~bb;
+          for (int bit = 0; bit < kPartMaxBits; ++bit) {
+            if (bit < hb) {
+              const unsigned bb = __ballot_sync(0xffffffffu, (dg >> bit) & 1);
+              peers &= ((dg >> bit) & 1) ? bb : ~bb;
+            }
           }
           const int rank = __popc(peers & ((1u << lane) - 1u));
           const int b = has ? myh[dg] : 0;
@@ -766,12 +814,13 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
         }
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < kSortWarps * kRadixBins; i += blockDim.x) rh[i] = 0;  // next-next pass
+      if (!part)
+        for (int i = threadIdx.x; i < kSortWarps * kRadixBins; i += blockDim.x) rh[i] = 0;  // next-next pass
       int2* t = src;
       src = dst;
       dst = t;
     }
-    // ---- 4. in-order run sums -> compact (value, id) list in dst ----
+    // ---- 4. sums in probe order -> compact (value, id) list in dst ----
     if (threadIdx.x == 0) {
       scratch[8] = 0u;
       scratch[9] = 0xffffffffu;  // min key of the sums
@@ -779,53 +828,136 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     }
     __syncthreads();
     uint32_t klo = 0xffffffffu, khi = 0u;
-    // each warp takes 32 consecutive elements per step; the previous id comes
-    // from the neighbour lane, so a step needs one load per lane (and a run
-    // that continues past the step is walked by its head lane)
-    for (int c0 = warp * 32 * kU; c0 < E; c0 += kSortWarps * 32 * kU) {
-      int2 v[kU];
-      int prev0 = -1;
+    if (part) {
+      // each warp: the partitions [Pa, Pb), a contiguous run [e0, e1) of src;
+      // its sums go to dst[e0 ..) first and are packed together afterwards
+      const int TR = 1 << tb;
+      float* tab = reinterpret_cast<float*>(sm + Lq.rhist) + (size_t)warp * kPartTable;
+      uint8_t* tag = reinterpret_cast<uint8_t*>(sm + Lq.rhist + kPartTagOff) + (size_t)warp * kPartTable;
+      float* stv = reinterpret_cast<float*>(sm + Lq.rhist + kPartStageOff) + warp * 64;
+      int* stt = reinterpret_cast<int*>(stv + 32);
+      for (int i = lane; i < kPartTable / 4; i += 32) reinterpret_cast<uint32_t*>(tag)[i] = 0u;
+      if (lane == 0) wcnt[warp] = 0;
+      __syncwarp();
+      const int Pa = (int)((long)warp * nbins / kSortWarps);
+      const int Pb = (int)((long)(warp + 1) * nbins / kSortWarps);
+      const int e0 = pstart[Pa], e1 = pstart[Pb];
+      int2* wout = dst + e0;
+      // write out the finished sum of slot `loc` (tag tg: partition Pa + tg - 1)
+      auto emit = [&](int tg, int loc, float sum) {
+        const int pos = atomicAdd(&wcnt[warp], 1);
+        wout[pos] = make_int2(((Pa + tg - 1) << tb) | loc, __float_as_int(sum));
+        klo = min(klo, fkey(sum));
+        khi = max(khi, fkey(sum));
+      };
+      for (int c0 = e0; c0 < e1; c0 += 32 * kU) {
+        int2 v[kU];
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int i = c0 + 32 * u + lane;
-        v[u] = i < E ? src[i] : make_int2(-1, 0);
-      }
-      if (lane == 0 && c0 > 0) prev0 = src[c0 - 1].x;
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int i = c0 + 32 * u + lane;
-        int prev = __shfl_up_sync(0xffffffffu, v[u].x, 1);
-        const int last = __shfl_sync(0xffffffffu, v[u > 0 ? u - 1 : 0].x, 31);
-        if (lane == 0) prev = u == 0 ? prev0 : last;
-        const int id = v[u].x;
-        const bool head = i < E && id < npts && id != prev;
-        float sum = head ? __int_as_float(v[u].y) : 0.0f;
-        // add the run's following values in order: first from the next lanes
-        // (shuffles), then, for a run that reaches the end of these 32, from memory
-        if (head) {
-          // the run's following values, in order; four pairs per round trip
-          int j = i + 1;
-          bool go = true;
-          while (go && j < E) {
-            int2 w[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) w[t] = j + t < E ? src[j + t] : make_int2(-1, 0);
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-              if (go && w[t].x == id) {
-                sum = sum + __int_as_float(w[t].y);
-              } else {
-                go = false;
-              }
-            }
-            j += 4;
-          }
+        for (int u = 0; u < kU; ++u) {
+          const int i = c0 + 32 * u + lane;
+          v[u] = i < e1 ? src[i] : make_int2(npts, 0);
         }
-        const uint32_t pos = warp_reserve(head, &scratch[8]);
-        if (head) {
-          dst[pos] = make_int2(id, __float_as_int(sum));
-          klo = min(klo, fkey(sum));
-          khi = max(khi, fkey(sum));
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          if (c0 + 32 * u >= e1) break;
+          const int id = v[u].x;
+          const bool act = id < npts;  // past e1 or a stale row: nothing to add
+          const int loc = id & (TR - 1);
+          stv[lane] = __int_as_float(v[u].y);
+          stt[lane] = (id >> tb) - Pa + 1;
+          // lanes on the same slot: the lowest applies them all, in lane
+          // (= partition, then probe) order
+          const unsigned peers = __match_any_sync(0xffffffffu, act ? loc : TR + lane);
+          __syncwarp();
+          if (act && __ffs(peers) - 1 == lane) {
+            int ct = tag[loc];
+            float t = tab[loc];
+            unsigned rest = peers;
+            do {
+              const int l = __ffs(rest) - 1;
+              rest &= rest - 1u;
+              const int tm = stt[l];
+              const float vm = stv[l];
+              if (tm == ct) {
+                t = t + vm;
+              } else {
+                if (ct != 0) emit(ct, loc, t);
+                ct = tm;
+                t = vm;  // first value of the id as is
+              }
+            } while (rest);
+            tag[loc] = (uint8_t)ct;
+            tab[loc] = t;
+          }
+          __syncwarp();
+        }
+      }
+      // the slots still held
+      for (int loc = lane; loc < TR; loc += 32) {
+        const int ct = tag[loc];
+        if (ct != 0) emit(ct, loc, tab[loc]);
+      }
+      __syncthreads();
+      // pack the warps' runs of sums together (into src, which is free now)
+      int off = 0;
+      for (int w = 0; w < warp; ++w) off += wcnt[w];
+      const int cnt = wcnt[warp];
+      for (int i = lane; i < cnt; i += 32) src[off + i] = wout[i];
+      if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < kSortWarps; ++w) tot += wcnt[w];
+        scratch[8] = (uint32_t)tot;
+      }
+      int2* t = src;
+      src = dst;
+      dst = t;
+    } else {
+      // each warp takes 32 consecutive elements per step; the previous id
+      // comes from the neighbour lane, so a step needs one load per lane (and
+      // a run that continues past the step is walked by its head lane)
+      for (int c0 = warp * 32 * kU; c0 < E; c0 += kSortWarps * 32 * kU) {
+        int2 v[kU];
+        int prev0 = -1;
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = c0 + 32 * u + lane;
+          v[u] = i < E ? src[i] : make_int2(-1, 0);
+        }
+        if (lane == 0 && c0 > 0) prev0 = src[c0 - 1].x;
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int i = c0 + 32 * u + lane;
+          int prev = __shfl_up_sync(0xffffffffu, v[u].x, 1);
+          const int last = __shfl_sync(0xffffffffu, v[u > 0 ? u - 1 : 0].x, 31);
+          if (lane == 0) prev = u == 0 ? prev0 : last;
+          const int id = v[u].x;
+          const bool head = i < E && id < npts && id != prev;
+          float sum = head ? __int_as_float(v[u].y) : 0.0f;
+          if (head) {
+            // the run's following values, in order; four pairs per round trip
+            int j = i + 1;
+            bool go = true;
+            while (go && j < E) {
+              int2 w[4];
+#pragma unroll
+              for (int t = 0; t < 4; ++t) w[t] = j + t < E ? src[j + t] : make_int2(-1, 0);
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                if (go && w[t].x == id) {
+                  sum = sum + __int_as_float(w[t].y);
+                } else {
+                  go = false;
+                }
+              }
+              j += 4;
+            }
+          }
+          const uint32_t pos = warp_reserve(head, &scratch[8]);
+          if (head) {
+            dst[pos] = make_int2(id, __float_as_int(sum));
+            klo = min(klo, fkey(sum));
+            khi = max(khi, fkey(sum));
+          }
         }
       }
     }
