@@ -51,6 +51,65 @@ CEOS_DEV bool tau_certifies(uint2 t, float v, int id) {
 }
 CEOS_DEV float key_val(uint64_t k) { return fkey_inv((uint32_t)(k >> 32)); }
 
+// Smallest float b with fkey(v) >= k  =>  v >= b for every non-NaN v: the
+// float of the key itself, -inf for keys at or below fkey(-inf) and +inf for
+// keys above fkey(+inf). The only non-NaN v with v >= b but fkey(v) < k is
+// v = -0 when b = +0, so a float test against b is a superset test.
+CEOS_DEV float key_lower_bound(uint32_t k) {
+  if (k <= 0x007fffffu) return __uint_as_float(0xff800000u);  // -inf
+  if (k > 0xff800000u) return __uint_as_float(0x7f800000u);   // +inf
+  return fkey_inv(k);
+}
+// Float prefilter of a (close, far) threshold pair: fkey(v) >= t.x implies
+// v >= bounds.x, and fkey(-v) >= t.y implies v <= bounds.y.
+CEOS_DEV float2 emit_bounds(uint2 t) {
+  return make_float2(key_lower_bound(t.x), -key_lower_bound(t.y));
+}
+
+// One digit step of a radix select, run by warp 0 of the block on a complete
+// 256-bin histogram: finds the bin b where the count of keys taken from the
+// top reaches `remaining` and writes scratch[0] = b, scratch[1] = keys in bins
+// above b, scratch[2] = keys in b, scratch[3] = all keys in the histogram.
+__device__ inline void radix_scan_hist(const uint32_t* hist, uint32_t remaining,
+                                       uint32_t* scratch) {
+  // lane l owns bins [8l, 8l+8)
+  const int lane = threadIdx.x & 31;
+  uint32_t loc[8];
+  uint32_t s = 0;
+#pragma unroll
+  for (int j = 7; j >= 0; --j) {
+    loc[j] = hist[lane * 8 + j];
+    s += loc[j];
+  }
+  // inclusive suffix sum of per-lane totals (lanes above me)
+  uint32_t t = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t v = __shfl_down_sync(0xffffffffu, t, o);
+    if (lane + o < 32) t += v;
+  }
+  uint32_t acc = t - s;  // count in bins of higher lanes
+  int found = -1;
+  uint32_t before = 0, inbin = 0;
+#pragma unroll
+  for (int j = 7; j >= 0; --j) {
+    if (found < 0 && acc + loc[j] >= remaining && acc < remaining) {
+      found = lane * 8 + j;
+      before = acc;
+      inbin = loc[j];
+    }
+    acc += loc[j];
+  }
+  if (found >= 0) {
+    scratch[0] = (uint32_t)found;
+    scratch[1] = before;
+    scratch[2] = inbin;
+  }
+  // total < remaining (fewer keys than requested): the caller takes them all
+  const uint32_t total = __shfl_sync(0xffffffffu, t, 0);
+  if (lane == 0) scratch[3] = total;
+}
+
 // ---------------------------------------------------------------------------
 // Block-level radix select.
 //
@@ -77,47 +136,7 @@ __device__ KeyT block_radix_threshold(GetKey get, long N, int K, uint32_t* hist,
       if (k != 0 && (k & mask) == prefix) atomicAdd(&hist[(uint32_t)(k >> shift) & 255u], 1u);
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-      // Suffix scan over 256 bins by one warp: lane l owns bins [8l, 8l+8).
-      const int lane = threadIdx.x;
-      uint32_t loc[8];
-      uint32_t s = 0;
-#pragma unroll
-      for (int j = 7; j >= 0; --j) {
-        loc[j] = hist[lane * 8 + j];
-        s += loc[j];
-      }
-      // inclusive suffix sum of per-lane totals (lanes above me)
-      uint32_t above = 0;
-      uint32_t t = s;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_down_sync(0xffffffffu, t, o);
-        if (lane + o < 32) t += v;
-      }
-      above = t - s;  // count in bins of higher lanes
-      // find the bin b where cumulative count from the top reaches `remaining`
-      uint32_t acc = above;
-      int found = -1;
-      uint32_t before = 0, inbin = 0;
-#pragma unroll
-      for (int j = 7; j >= 0; --j) {
-        if (found < 0 && acc + loc[j] >= remaining && acc < remaining) {
-          found = lane * 8 + j;
-          before = acc;
-          inbin = loc[j];
-        }
-        acc += loc[j];
-      }
-      if (found >= 0) {
-        scratch[0] = (uint32_t)found;
-        scratch[1] = before;
-        scratch[2] = inbin;
-      }
-      // total < remaining (N < K): handled below via scratch[3]
-      const uint32_t total = __shfl_sync(0xffffffffu, t, 0);
-      if (lane == 0) scratch[3] = total;
-    }
+    if (threadIdx.x < 32) radix_scan_hist(hist, remaining, scratch);
     __syncthreads();
     const uint32_t total = scratch[3];
     if (total < remaining) {

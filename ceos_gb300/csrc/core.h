@@ -332,7 +332,13 @@ struct Core {
       return fail(CEOS_ERR_ARG, "top_m (+ reserve) (%d) must be in [1, n_points=%ld]", m, n);
     if (m > 8192) return fail(CEOS_ERR_UNSUPPORTED, "top_m (+ reserve) > 8192 is not supported");
     // ---- sample thresholds ----
-    long S = n <= 65536 ? n : std::max(8192L, std::min(n / 8, 32L * m));
+    // A strided sample of S rows; the rank-r key of each column end in it is
+    // that end's emission threshold. The sample holds Binomial(S, m/n) of the
+    // end's true top m (mean mu = S m / n); the list comes out short only if
+    // more than r of them fall in the sample, which for r = mu + 5 sqrt(mu) + 8
+    // has a Poisson tail probability below 1e-8 per column end (a short list
+    // is then selected exactly, never wrong).
+    long S = n <= 65536 ? n : std::max(8192L, std::min(n / 8, 16L * m));
     if (S > n) S = n;
     const bool exact = (S == n);
     int rank;
@@ -342,13 +348,13 @@ struct Core {
       cap = std::max(128, np2(2 * m));
     } else {
       const double mu = (double)S * m / (double)n;
-      rank = (int)std::min((double)S, std::ceil(2.0 * mu + 4.0 * std::sqrt(mu) + 8.0));
+      rank = (int)std::min((double)S, std::ceil(mu + 5.0 * std::sqrt(mu) + 8.0));
       const double expected = (double)rank * (double)n / (double)S;
       cap = np2((int)std::min(1e9, std::max((double)m + 64.0, 2.0 * expected)));
       cap = std::min(cap, 16384L);
       if (cap < m + 1) cap = np2(m + 1);
     }
-    DevBuf samp, rowmap, th, cnt, cand, failb;
+    DevBuf samp, rowmap, th, thf, cnt, cand, failb;
     CUDA_TRY(samp.ensure((size_t)Cc * S * 4));
     if (!exact) {
       std::vector<long> rm(S);
@@ -360,11 +366,12 @@ struct Core {
     ProjArgs a = proj_base();
     a.row_map = exact ? nullptr : rowmap.as<long>();
     a.n_rows = S;
-    a.out = samp.as<float>();
-    a.ld_out = S;
-    CUDA_TRY(launch_project(a, PROJ_COLS, L, sms, stream));
+    a.out = samp.as<float>();  // row-major [S][C]
+    CUDA_TRY(launch_project(a, PROJ_ROWS, L, sms, stream));
     CUDA_TRY(th.ensure((size_t)Cc * 2 * 4));
-    CUDA_TRY(launch_sample_thresholds(samp.as<float>(), S, Cc, rank, th.as<uint32_t>(), stream));
+    CUDA_TRY(thf.ensure((size_t)Cc * sizeof(float2)));
+    CUDA_TRY(launch_sample_thresholds(samp.as<float>(), S, Cc, rank, th.as<uint32_t>(),
+                                      thf.as<float2>(), stream));
     timer.mark("sample+thresholds");
     // ---- fused projection + candidate emission ----
     CUDA_TRY(cnt.ensure((size_t)Cc * 2 * 4));
@@ -375,6 +382,7 @@ struct Core {
     ProjArgs e = proj_base();
     e.n_rows = n;
     e.th = th.as<uint32_t>();
+    e.thf = thf.as<float2>();
     e.cnt = cnt.as<unsigned>();
     e.cand = cand.as<uint64_t>();
     e.cap = (int)cap;

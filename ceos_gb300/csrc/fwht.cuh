@@ -54,6 +54,11 @@ CEOS_DEV int line_elem(int line, int e, int o, int b) {
   return low | (e << o) | (high << (o + b));
 }
 
+// The line's part and the element's part of an index occupy disjoint bits, so
+// padj(line_elem(line, e, o, b)) = padj(line_elem(line, 0, o, b)) + padj(e << o):
+// one base per line plus a compile-time offset per element.
+__host__ __device__ constexpr int padj_c(int j) { return j + ((j >> 5) << 2); }
+
 // Two butterflies at once: (a0, c0) and (a1, c1) become (a0+c0, a0-c0) and
 // (a1+c1, a1-c1), as packed f32x2 adds/subtracts (two IEEE round-to-nearest
 // operations each, so the results are those of the scalar form).
@@ -107,13 +112,13 @@ CEOS_DEV void fwht_phase(float* dst, int lane) {
     const int task = lane + 32 * t;
     const int vec = task / lines;
     const int line = task % lines;
-    float* d = dst + vec * Cfg::Vstride;
+    float* d = dst + vec * Cfg::Vstride + padj(line_elem(line, 0, o, B));
     float v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = d[padj(line_elem(line, e, o, B))];
+    for (int e = 0; e < E; ++e) v[e] = d[padj_c(e << o)];
     reg_stages<B>(v);
 #pragma unroll
-    for (int e = 0; e < E; ++e) d[padj(line_elem(line, e, o, B))] = v[e];
+    for (int e = 0; e < E; ++e) d[padj_c(e << o)] = v[e];
   }
   if constexpr (p + 1 < Cfg::P) fwht_phase<L, p + 1>(dst, lane);
 }
@@ -167,6 +172,92 @@ CEOS_DEV void fwht_round(const float* src, float* dst, const uint32_t* sw, int l
     }
   }
   if constexpr (Cfg::P > 1) fwht_phase<L, 1>(dst, lane);
+  __syncwarp();
+}
+
+// Phases p.. of a round whose last phase may hand its lines to a consumer
+// instead of storing them: when `emit` is set, phase P-1 calls
+// out(vec, line, v) with the E = 2^bits(P-1) outputs of each of the lane's
+// lines in registers; element e of the line is output
+// line_elem(line, e, off(P-1), bits(P-1)) of vector vec. When `emit` is clear
+// the round stores its outputs like fwht_round (the branch is warp-uniform).
+template <int L, int p, class Out>
+CEOS_DEV void fwht_phase_out(float* dst, int lane, bool emit, Out& out) {
+  using Cfg = FwhtCfg<L>;
+  constexpr int o = Cfg::off(p);
+  constexpr int B = Cfg::bits(p);
+  constexpr int E = 1 << B;
+  constexpr int lines = Cfg::F / E;
+  constexpr bool last = (p + 1 == Cfg::P);
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < Cfg::tasks(p); ++t) {
+    const int task = lane + 32 * t;
+    const int vec = task / lines;
+    const int line = task % lines;
+    float* d = dst + vec * Cfg::Vstride + padj(line_elem(line, 0, o, B));
+    float v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = d[padj_c(e << o)];
+    reg_stages<B>(v);
+    if (last && emit) {
+      out(vec, line, v);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) d[padj_c(e << o)] = v[e];
+    }
+  }
+  if constexpr (!last) fwht_phase_out<L, p + 1>(dst, lane, emit, out);
+}
+
+// fwht_round whose last phase feeds `out` (see fwht_phase_out) when `emit`.
+template <int L, class Out>
+CEOS_DEV void fwht_round_out(const float* src, float* dst, const uint32_t* sw, int lane, bool emit,
+                             Out& out) {
+  using Cfg = FwhtCfg<L>;
+  constexpr int B = Cfg::bits(0);
+  constexpr int E = 1 << B;
+  constexpr int lines0 = Cfg::F / E;
+  constexpr bool last = (Cfg::P == 1);
+#pragma unroll
+  for (int t = 0; t < Cfg::tasks(0); ++t) {
+    const int task = lane + 32 * t;
+    const int vec = task / lines0;
+    const int line = task % lines0;
+    const int j0 = line * E;
+    const float* s = src + vec * Cfg::Vstride + padj(j0);
+    float* d = dst + vec * Cfg::Vstride + padj(j0);
+    const uint32_t nword = ~(sw[j0 >> 5] >> (j0 & 31));  // bit e set => flip
+    float v[E];
+    if constexpr (E >= 4) {
+#pragma unroll
+      for (int k = 0; k < E / 4; ++k) {
+        const float4 q = reinterpret_cast<const float4*>(s)[k];
+        v[4 * k] = q.x;
+        v[4 * k + 1] = q.y;
+        v[4 * k + 2] = q.z;
+        v[4 * k + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = s[e];
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      v[e] = __uint_as_float(__float_as_uint(v[e]) ^ ((nword << (31 - e)) & 0x80000000u));
+    reg_stages<B>(v);
+    if (last && emit) {
+      out(vec, line, v);
+    } else if constexpr (E >= 4) {
+#pragma unroll
+      for (int k = 0; k < E / 4; ++k)
+        reinterpret_cast<float4*>(d)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) d[e] = v[e];
+    }
+  }
+  if constexpr (Cfg::P > 1) fwht_phase_out<L, 1>(dst, lane, emit, out);
   __syncwarp();
 }
 

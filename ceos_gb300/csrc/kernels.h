@@ -24,6 +24,9 @@ struct ProjArgs {
   const int* col_slot = nullptr;  // PROJ_COLS: column -> output slot (-1 = skip); null = identity
   // PROJ_EMIT
   const uint32_t* th = nullptr;  // [C][2] key thresholds (close: fkey(v), far: fkey(-v))
+  // [C] float prefilter of th: a value v can clear the close end only if
+  // v >= thf.x and the far end only if v <= thf.y (see emit_bounds)
+  const float2* thf = nullptr;
   unsigned* cnt = nullptr;       // [C][2] candidate counters
   uint64_t* cand = nullptr;      // [C][2][cap] packed keys
   int cap = 0;
@@ -39,9 +42,10 @@ bool project_tc_supported(int L);
 cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st);
 
 // ---- selection (select.cu) ----
-// Per column: u32 thresholds so that about `rank` sample values pass each end.
+// Per column: u32 thresholds so that about `rank` sample values pass each end,
+// and their float prefilter bounds (thf, see ProjArgs::thf).
 cudaError_t launch_sample_thresholds(const float* samp, long S, int C, int rank, uint32_t* th,
-                                     cudaStream_t st);
+                                     float2* thf, cudaStream_t st);
 // Per column end: top-m of the emitted candidates -> buckets; flags failures.
 cudaError_t launch_finish_buckets(const uint64_t* cand, const unsigned* cnt, int cap, int C, int m,
                                   int* bids, float* bvals, unsigned* fail, cudaStream_t st);

@@ -18,6 +18,7 @@
 //          the n x (R*D) projection matrix never travels to HBM.
 #include "kernels.h"
 #include "fwht.cuh"
+#include "emit.cuh"
 
 namespace ceos {
 
@@ -103,45 +104,62 @@ __global__ void __launch_bounds__(256, RegRow<L>::ok ? 3 : 1) k_project(ProjArgs
     __syncwarp();
     for (int r = 0; r < a.R; ++r) {
       const uint32_t* sw = s_signs + (size_t)r * 3 * words;
-      if constexpr (kRegRow) {
-        fwht_round_regs<L>(xr, wbuf, sw, lane);
-#pragma unroll 1
-        for (int i = 1; i < 3; ++i) fwht_round<L>(wbuf, wbuf, sw + i * words, lane);
-      } else {
-#pragma unroll 1
-        for (int i = 0; i < 3; ++i) fwht_round<L>(i == 0 ? xbuf : wbuf, wbuf, sw + i * words, lane);
-      }
-      // outputs j < D of each vector, consecutive lanes on consecutive columns
-#pragma unroll 1
-      for (int vec = 0; vec < Cfg::V; ++vec) {
+      // Consumer of the last phase of round 2: the lane's output lines in
+      // registers, element e of a line at column offset j0 + (e << o).
+      auto out = [&](int vec, int line, auto& v) {
+        constexpr int o = Cfg::off(Cfg::P - 1);
+        constexpr int B = Cfg::bits(Cfg::P - 1);
+        constexpr int E = 1 << B;
         const long row = row0 + vec;
-        if (row >= a.n_rows) break;
-        const float* w = wbuf + vec * Cfg::Vstride;
-        long id = 0;
-        if constexpr (MODE == PROJ_EMIT) id = a.id_base + (a.row_map ? a.row_map[row] : row);
-        for (int j = lane; j < a.D; j += 32) {
-          const float v = w[padj(j)];
-          const int col = r * a.D + j;
-          if constexpr (MODE == PROJ_ROWS) {
-            a.out[row * (long)C + col] = v;
-          } else if constexpr (MODE == PROJ_COLS) {
-            const int slot = a.col_slot ? a.col_slot[col] : col;
-            if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v;
-          } else {  // PROJ_EMIT
-            if (a.col_active && !a.col_active[col]) continue;
-            const uint2 th = __ldg(reinterpret_cast<const uint2*>(a.th) + col);
-            if (fkey(v) >= th.x) {
-              const unsigned pos = atomicAdd(&a.cnt[2 * col], 1u);
-              if (pos < (unsigned)a.cap) a.cand[((long)2 * col) * a.cap + pos] = pack_key(v, (int)id);
-            }
-            if (fkey(-v) >= th.y) {
-              const unsigned pos = atomicAdd(&a.cnt[2 * col + 1], 1u);
-              if (pos < (unsigned)a.cap)
-                a.cand[((long)2 * col + 1) * a.cap + pos] = pack_key(-v, (int)id);
+        if (row >= a.n_rows) return;
+        const int j0 = line_elem(line, 0, o, B);
+        const bool all_cols = (a.D == Cfg::F);  // else keep outputs j < D only
+        if constexpr (MODE == PROJ_ROWS) {
+          float* dst = a.out + row * (long)C + r * a.D + j0;
+#pragma unroll
+          for (int e = 0; e < E; ++e)
+            if (all_cols || j0 + (e << o) < a.D) dst[e << o] = v[e];
+        } else if constexpr (MODE == PROJ_COLS) {
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+            const int j = j0 + (e << o);
+            if (all_cols || j < a.D) {
+              const int col = r * a.D + j;
+              const int slot = a.col_slot ? a.col_slot[col] : col;
+              if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v[e];
             }
           }
+        } else {  // PROJ_EMIT
+          // float prefilter of every output into a bit mask, then the exact
+          // test of the (few) flagged outputs, read back through this lane's
+          // own slots of the vector buffer
+          const float2* tb = a.thf + r * a.D + j0;
+          uint32_t hit = 0;
+#pragma unroll
+          for (int e = 0; e < E; ++e)
+            if (all_cols || j0 + (e << o) < a.D)
+              if (emit_maybe(v[e], __ldg(tb + (e << o)))) hit |= 1u << e;
+          if (hit) {
+            float* w = wbuf + vec * Cfg::Vstride;
+#pragma unroll
+            for (int e = 0; e < E; ++e) w[padj(j0) + padj_c(e << o)] = v[e];
+            const int id = (int)(a.id_base + (a.row_map ? a.row_map[row] : row));
+            do {
+              const int e = __ffs((int)hit) - 1;
+              hit &= hit - 1;
+              const int j = j0 + (e << o);
+              emit_exact(a, r * a.D + j, w[padj(j)], id);
+            } while (hit);
+          }
         }
+      };
+      if constexpr (kRegRow) {
+        fwht_round_regs<L>(xr, wbuf, sw, lane);
+      } else {
+        fwht_round<L>(xbuf, wbuf, sw, lane);
       }
+#pragma unroll 1
+      for (int i = 1; i < 3; ++i) fwht_round_out<L>(wbuf, wbuf, sw + i * words, lane, i == 2, out);
       __syncwarp();
     }
   }

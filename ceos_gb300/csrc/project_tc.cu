@@ -27,6 +27,7 @@
 // register-resident chain here has no such traffic.
 #include "kernels.h"
 #include "common.cuh"
+#include "emit.cuh"
 
 namespace ceos {
 
@@ -210,18 +211,8 @@ __global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
             } else if constexpr (MODE == PROJ_COLS) {
               const int slot = a.col_slot ? a.col_slot[col] : col;
               if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v;
-            } else {  // PROJ_EMIT
-              if (a.col_active && !a.col_active[col]) continue;
-              const uint2 th = __ldg(reinterpret_cast<const uint2*>(a.th) + col);
-              if (fkey(v) >= th.x) {
-                const unsigned pos = atomicAdd(&a.cnt[2 * col], 1u);
-                if (pos < (unsigned)a.cap) a.cand[((long)2 * col) * a.cap + pos] = pack_key(v, (int)id);
-              }
-              if (fkey(-v) >= th.y) {
-                const unsigned pos = atomicAdd(&a.cnt[2 * col + 1], 1u);
-                if (pos < (unsigned)a.cap)
-                  a.cand[((long)2 * col + 1) * a.cap + pos] = pack_key(-v, (int)id);
-              }
+            } else {  // PROJ_EMIT: float prefilter, then the exact key test
+              if (emit_maybe(v, __ldg(a.thf + col))) emit_exact(a, col, v, (int)id);
             }
           }
     }

@@ -5,7 +5,7 @@
 // The reference keeps two bounded min-heaps per column while scanning all n
 // projections. Here the selection is split so that the full projection
 // matrix is never stored:
-//   1. sample thresholds: a strided sample of S rows is projected (PROJ_COLS)
+//   1. sample thresholds: a strided sample of S rows is projected (PROJ_ROWS)
 //      and, per column, the rank-r_s value of each end is taken as a key
 //      threshold (k_sample_thresholds). When S = n the threshold is exact.
 //   2. the full projection runs in PROJ_EMIT mode, appending every value whose
@@ -21,25 +21,99 @@
 
 namespace ceos {
 
-__global__ void __launch_bounds__(256) k_sample_thresholds(const float* samp, long S, int rank,
-                                                          uint32_t* th) {
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t scratch[8];
-  const int c = blockIdx.x;
-  const float* col = samp + (long)c * S;
-  const uint32_t t_hi = block_radix_threshold<uint32_t>(
-      [&](long i) { return fkey(col[i]); }, S, rank, hist, scratch);
-  const uint32_t t_lo = block_radix_threshold<uint32_t>(
-      [&](long i) { return fkey(-col[i]); }, S, rank, hist, scratch);
-  if (threadIdx.x == 0) {
-    th[2 * c] = t_hi;
-    th[2 * c + 1] = t_lo;
+// Sample thresholds. The S sampled rows' projections arrive row-major
+// (samp[i * C + col], coalesced writes from the projection). One block owns 32
+// adjacent columns: lane l of every warp handles column c0 + l, and warp w
+// reads rows w, w + 32, ..., so each warp load is one 128-byte line. Every
+// 8-bit digit pass builds, per column, the histograms of both ends at once:
+// the close end ranks k = fkey(v), the far end fkey(-v) = ~k. Histograms are
+// per column (padded to 257 bins, so lanes on equal digits hit different
+// banks); lanes of a warp never share a column, so increments only collide
+// across warps. The threshold of an end is the key of rank `rank` from its top
+// (every key when S <= rank). Which threshold a column gets changes how many
+// candidates the emission pass appends, never the selected buckets.
+constexpr int kThCols = 32;
+constexpr int kThWarps = 32;
+constexpr int kThBins = 257;
+
+__global__ void __launch_bounds__(kThWarps * 32) k_sample_thresholds(const float* samp, long S,
+                                                                    int C, int rank, uint32_t* th,
+                                                                    float2* thf) {
+  extern __shared__ __align__(16) uint32_t s_hist[];  // [2][kThCols][kThBins]
+  __shared__ uint32_t s_prefix[2][kThCols], s_remaining[2][kThCols], s_done[2][kThCols];
+  __shared__ uint32_t s_scratch[2][kThCols][4];
+  __shared__ int s_all_done;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c0 = blockIdx.x * kThCols;
+  const int col = c0 + lane;
+  const bool all = rank <= 0 || S <= rank;  // every sampled key passes
+  if (threadIdx.x < 2 * kThCols) {
+    const int end = threadIdx.x / kThCols, c = threadIdx.x % kThCols;
+    s_prefix[end][c] = 0u;
+    s_remaining[end][c] = (uint32_t)(rank > 0 ? rank : 0);
+    s_done[end][c] = (all || c0 + c >= C) ? 1u : 0u;
+  }
+  if (threadIdx.x == 0) s_all_done = all ? 1 : 0;
+  __syncthreads();
+  uint32_t mask = 0u;
+  for (int shift = 24; shift >= 0 && !s_all_done; shift -= 8) {
+    for (int b = threadIdx.x; b < 2 * kThCols * kThBins; b += blockDim.x) s_hist[b] = 0u;
+    __syncthreads();
+    const bool act0 = !s_done[0][lane], act1 = !s_done[1][lane];
+    const uint32_t p0 = s_prefix[0][lane], p1 = s_prefix[1][lane];
+    uint32_t* h0 = s_hist + lane * kThBins;
+    uint32_t* h1 = s_hist + (kThCols + lane) * kThBins;
+    if (col < C && (act0 || act1)) {
+      const float* src = samp + col;
+      for (long i = warp; i < S; i += kThWarps) {
+        const uint32_t k = fkey(__ldg(src + i * C));
+        if (act0 && (k & mask) == p0) atomicAdd(h0 + ((k >> shift) & 255u), 1u);
+        if (act1 && (~k & mask) == p1) atomicAdd(h1 + ((~k >> shift) & 255u), 1u);
+      }
+    }
+    __syncthreads();
+    // warp w scans column w, both ends
+    for (int end = 0; end < 2; ++end)
+      if (!s_done[end][warp])
+        radix_scan_hist(s_hist + (end * kThCols + warp) * kThBins, s_remaining[end][warp],
+                        s_scratch[end][warp]);
+    __syncthreads();
+    if (threadIdx.x < 2 * kThCols) {
+      const int end = threadIdx.x / kThCols, c = threadIdx.x % kThCols;
+      if (!s_done[end][c]) {
+        // the histogram held every remaining key of this end and more than
+        // `remaining` of them, so a bin was found
+        const uint32_t* sc = s_scratch[end][c];
+        s_prefix[end][c] |= sc[0] << shift;
+        s_remaining[end][c] -= sc[1];
+        if (sc[2] == s_remaining[end][c]) s_done[end][c] = 1u;
+      }
+    }
+    mask |= 255u << shift;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int d = 1;
+      for (int c = 0; c < 2 * kThCols; ++c) d &= (int)s_done[c / kThCols][c % kThCols];
+      s_all_done = d;
+    }
+    __syncthreads();
+  }
+  if (warp == 0 && col < C) {
+    const uint2 t = all ? make_uint2(0u, 0u) : make_uint2(s_prefix[0][lane], s_prefix[1][lane]);
+    th[2 * col] = t.x;
+    th[2 * col + 1] = t.y;
+    thf[col] = emit_bounds(t);
   }
 }
 
 cudaError_t launch_sample_thresholds(const float* samp, long S, int C, int rank, uint32_t* th,
-                                     cudaStream_t st) {
-  k_sample_thresholds<<<C, 256, 0, st>>>(samp, S, rank, th);
+                                     float2* thf, cudaStream_t st) {
+  const size_t smem = (size_t)2 * kThCols * kThBins * 4;
+  cudaError_t e = cudaFuncSetAttribute(k_sample_thresholds,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_sample_thresholds<<<(C + kThCols - 1) / kThCols, kThWarps * 32, smem, st>>>(samp, S, C, rank,
+                                                                              th, thf);
   return cudaGetLastError();
 }
 
