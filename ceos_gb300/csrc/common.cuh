@@ -243,11 +243,24 @@ CEOS_DEV uint32_t warp_reserve(bool want, uint32_t* counter) {
 
 // pre (optional): min key, max key and count of the valid items, already
 // known to the caller; pass 1 is then skipped.
-template <typename GetItem>
+//
+// kBinOrder: on the histogram path, items above the threshold bin are
+// scattered to the output segment of their bin (bins in descending order,
+// offsets from the suffix scan of the histogram) instead of being appended,
+// and each bin's few items are then insertion-sorted, so that `out` comes out
+// sorted descending without a block-wide sort. scratch[12] = 1 reports a
+// sorted result; it is 0 when a path without bin order was taken or a bin
+// holds more than kBinSortMax items (the caller sorts then).
+constexpr int kBinSortMax = 24;
+template <bool kBinOrder = false, typename GetItem>
 __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32_t* hist,
                                uint64_t* maybe, int maybe_cap, uint32_t* scratch,
                                const uint32_t* pre = nullptr) {
   const int lane = threadIdx.x & 31;
+  if (kBinOrder && threadIdx.x == 0) {
+    scratch[12] = 0u;
+    scratch[13] = 0u;
+  }
   // ---- pass 1: min / max keys and count ----
   if (threadIdx.x == 0) {
     scratch[0] = pre ? pre[0] : 0xffffffffu;  // min key
@@ -383,6 +396,9 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
         scratch[6] = acc;  // items above the threshold bin
         scratch[7] = h;    // items in it
       }
+      // bin order: the bin's output offset (items in higher bins) becomes its
+      // scatter cursor (each thread rewrites only its own bins)
+      if constexpr (kBinOrder) hist[b0 + j] = acc;
       acc += h;
     }
   }
@@ -408,12 +424,19 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
       const int b = ok[u] ? bin_of(v[u]) : -1;
       const bool sure = ok[u] && b > tb;
       const bool cand = ok[u] && b == tb && fits;
-      const uint32_t p1 = warp_reserve(sure, &scratch[3]);
-      if (sure) out[p1] = pack_key(v[u], id[u]);
+      if constexpr (kBinOrder) {
+        if (sure) out[atomicAdd(&hist[b], 1u)] = pack_key(v[u], id[u]);
+      } else {
+        const uint32_t p1 = warp_reserve(sure, &scratch[3]);
+        if (sure) out[p1] = pack_key(v[u], id[u]);
+      }
       const uint32_t p2 = warp_reserve(cand, &scratch[4]);
       if (cand) maybe[p2] = pack_key(v[u], id[u]);
     }
   }
+  // bin order scattered the items above the threshold bin to out[0, above)
+  // without the append counter; later appends go after them
+  if (kBinOrder && threadIdx.x == 0) scratch[3] = above;
   __syncthreads();
   if (fits) {
     int np = 1;
@@ -422,6 +445,27 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
     __syncthreads();
     block_bitonic_sort_desc(maybe, np);
     for (uint32_t i = threadIdx.x; i < need; i += blockDim.x) out[above + i] = maybe[i];
+    if constexpr (kBinOrder) {
+      // bin b > tb now holds out[end(b + 1), end(b)), end = its final cursor
+      for (int b = tb + 1 + threadIdx.x; b < kHistBins; b += blockDim.x) {
+        const uint32_t lo = (b + 1 < kHistBins) ? hist[b + 1] : 0u, hi = hist[b];
+        if (hi - lo > (uint32_t)kBinSortMax) {
+          scratch[13] = 1u;
+          continue;
+        }
+        for (uint32_t i = lo + 1; i < hi; ++i) {
+          const uint64_t x = out[i];
+          uint32_t j = i;
+          while (j > lo && out[j - 1] < x) {
+            out[j] = out[j - 1];
+            --j;
+          }
+          out[j] = x;
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) scratch[12] = scratch[13] ? 0u : 1u;
+    }
     __syncthreads();
   } else {
     // threshold bin too large for the buffer: radix select inside it
@@ -444,15 +488,19 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
 }
 
 // block_topk_hist followed by a descending sort: out[0..ret) best first,
-// out[ret..out_cap) zero. out_cap is a power of two >= K.
-template <typename GetItem>
+// out[ret..out_cap) zero. out_cap is a power of two >= K. kBinOrder (for large
+// K, e.g. bucket lists) orders the result by histogram bins and sorts within
+// bins, falling back to the block-wide bitonic sort; small K (probes, final
+// top-k) is cheaper with the bitonic sort alone.
+template <bool kBinOrder = false, typename GetItem>
 __device__ int block_topk_hist_sorted(GetItem get, long N, int K, uint64_t* out, int out_cap,
                                       uint32_t* hist, uint64_t* maybe, int maybe_cap,
                                       uint32_t* scratch) {
-  const int cnt = block_topk_hist(get, N, K, out, hist, maybe, maybe_cap, scratch);
+  const int cnt = block_topk_hist<kBinOrder>(get, N, K, out, hist, maybe, maybe_cap, scratch);
+  const bool sorted = kBinOrder && scratch[12] != 0u;
   for (int i = cnt + threadIdx.x; i < out_cap; i += blockDim.x) out[i] = 0ull;
   __syncthreads();
-  block_bitonic_sort_desc(out, out_cap);
+  if (!sorted) block_bitonic_sort_desc(out, out_cap);
   return cnt;
 }
 

@@ -23,15 +23,17 @@ namespace ceos {
 
 // Sample thresholds. The S sampled rows' projections arrive row-major
 // (samp[i * C + col], coalesced writes from the projection). One block owns 32
-// adjacent columns: lane l of every warp handles column c0 + l, and warp w
-// reads rows w, w + 32, ..., so each warp load is one 128-byte line. Every
-// 8-bit digit pass builds, per column, the histograms of both ends at once:
-// the close end ranks k = fkey(v), the far end fkey(-v) = ~k. Histograms are
+// adjacent columns: lane l of every warp handles column c0 + l, and warp w of
+// kThWarps reads rows w, w + kThWarps, ..., so each warp load is one 128-byte
+// line. Every 8-bit digit pass builds, per column, the histograms of both
+// ends at once: the close end ranks k = fkey(v), the far end fkey(-v) = ~k.
+// Histograms are
 // per column (padded to 257 bins, so lanes on equal digits hit different
 // banks); lanes of a warp never share a column, so increments only collide
-// across warps. The threshold of an end is the key of rank `rank` from its top
-// (every key when S <= rank). Which threshold a column gets changes how many
-// candidates the emission pass appends, never the selected buckets.
+// across warps. The threshold of an end is the lower edge of the 16-bit key
+// prefix that holds its rank-`rank` key from the top (every key when
+// S <= rank). Which threshold a column gets changes how many candidates the
+// emission pass appends, never the selected buckets.
 constexpr int kThCols = 32;
 constexpr int kThWarps = 32;
 constexpr int kThBins = 257;
@@ -56,7 +58,10 @@ __global__ void __launch_bounds__(kThWarps * 32) k_sample_thresholds(const float
   if (threadIdx.x == 0) s_all_done = all ? 1 : 0;
   __syncthreads();
   uint32_t mask = 0u;
-  for (int shift = 24; shift >= 0 && !s_all_done; shift -= 8) {
+  // two digit passes: the threshold is the lower edge of the 16-bit key prefix
+  // holding the rank-`rank` key (a column end that resolves in the first pass
+  // gets its exact key), so at least `rank` sampled keys clear it
+  for (int shift = 24; shift >= 16 && !s_all_done; shift -= 8) {
     for (int b = threadIdx.x; b < 2 * kThCols * kThBins; b += blockDim.x) s_hist[b] = 0u;
     __syncthreads();
     const bool act0 = !s_done[0][lane], act1 = !s_done[1][lane];
@@ -72,11 +77,12 @@ __global__ void __launch_bounds__(kThWarps * 32) k_sample_thresholds(const float
       }
     }
     __syncthreads();
-    // warp w scans column w, both ends
-    for (int end = 0; end < 2; ++end)
-      if (!s_done[end][warp])
-        radix_scan_hist(s_hist + (end * kThCols + warp) * kThBins, s_remaining[end][warp],
-                        s_scratch[end][warp]);
+    // warp w scans columns w, w + kThWarps, ..., both ends
+    for (int c = warp; c < kThCols; c += kThWarps)
+      for (int end = 0; end < 2; ++end)
+        if (!s_done[end][c])
+          radix_scan_hist(s_hist + (end * kThCols + c) * kThBins, s_remaining[end][c],
+                          s_scratch[end][c]);
     __syncthreads();
     if (threadIdx.x < 2 * kThCols) {
       const int end = threadIdx.x / kThCols, c = threadIdx.x % kThCols;
@@ -142,7 +148,7 @@ __global__ void __launch_bounds__(256) k_finish_buckets(const uint64_t* cand, co
     return;
   }
   const uint64_t* list = cand + ce * cap;
-  block_topk_hist_sorted(
+  block_topk_hist_sorted<true>(
       [&](long i, float& v, int& id) {
         const uint64_t k = list[i];
         v = key_val(k);
@@ -187,7 +193,7 @@ __global__ void __launch_bounds__(512) k_exact_buckets(const float* vals, long n
   const long ce = 2L * col + end;
   if (!fail[ce]) return;
   const float* v = vals + (long)slot * ld;
-  block_topk_hist_sorted(
+  block_topk_hist_sorted<true>(
       [&](long i, float& x, int& id) {
         x = end ? -v[i] : v[i];
         id = (int)i;

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(512) k_stream_merge(int m, const float* newP, 
     id = (int)(cur + t);
     return true;
   };
-  const int cnt = block_topk_hist_sorted(get, (long)m + b, m, s_out, out_cap, hist, maybe,
+  const int cnt = block_topk_hist_sorted<true>(get, (long)m + b, m, s_out, out_cap, hist, maybe,
                                          kMergeMaybe, scratch);
   // the sort ends with a barrier, so every read of ids/vals is done
   for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(512) k_stream_merge_exact(int M, int m, const 
     id = (int)(cur + t);
     return true;
   };
-  const int got = block_topk_hist_sorted(get, (long)n_old + b, M, s_out, out_cap, hist, maybe,
+  const int got = block_topk_hist_sorted<true>(get, (long)n_old + b, M, s_out, out_cap, hist, maybe,
                                          kMergeMaybe, scratch);
   // the sorted result is certified up to its first entry below tau
   const uint2 t = tau[ce];
