@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
   constexpr int NT = FD / 8;   // 8-column tiles
   constexpr int KT = FD / 16;  // 16-deep k steps
   constexpr int WORDS = F / 32;
-  extern __shared__ __align__(16) uint32_t s_signs[];  // [R][3][WORDS]
+  extern __shared__ __align__(16) uint32_t s_signs[];  // [R][3][WORDS], then the emit scratch
   const int n_sign_words = a.R * 3 * WORDS;
   for (int i = threadIdx.x; i < n_sign_words; i += blockDim.x) s_signs[i] = a.signs[i];
   __syncthreads();
@@ -88,6 +88,8 @@ __global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
   const int warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const int C = a.R * a.D;
+  // PROJ_EMIT: per warp [32 elements][32 lanes] floats, this lane's column
+  float* s_scr = reinterpret_cast<float*>(s_signs + ((n_sign_words + 3) & ~3)) + warp * 32 * 32 + lane;
 
   // constant H fragments: B operand of X.H (k = rows of H, n = columns) and
   // A operand of H.Y
@@ -195,33 +197,66 @@ __global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
             }
           }
       }
-      // outputs j < D of repeat r
+      // outputs j < D of repeat r; element f = (mi * NT + ni) * 4 + e of the
+      // lane is output j = (16 mi + g + 8 (e >> 1)) * FD + 8 ni + 2 t + (e & 1)
+      const bool all_cols = (a.D == F);
+      if constexpr (MODE == PROJ_EMIT) {
+        // float prefilter into a bit mask, then the exact test of the flagged
+        // outputs, read back through this lane's column of the warp scratch
+        const float2* tb = a.thf + r * a.D;
+        uint32_t hit = 0;
 #pragma unroll
-      for (int mi = 0; mi < MT; ++mi)
+        for (int mi = 0; mi < MT; ++mi)
 #pragma unroll
-        for (int ni = 0; ni < NT; ++ni)
+          for (int ni = 0; ni < NT; ++ni)
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int j = (16 * mi + g + 8 * (e >> 1)) * FD + 8 * ni + 2 * t + (e & 1);
-            if (j >= a.D) continue;
-            const float v = z[mi][ni][e];
-            const int col = r * a.D + j;
-            if constexpr (MODE == PROJ_ROWS) {
-              a.out[row * (long)C + col] = v;
-            } else if constexpr (MODE == PROJ_COLS) {
-              const int slot = a.col_slot ? a.col_slot[col] : col;
-              if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v;
-            } else {  // PROJ_EMIT: float prefilter, then the exact key test
-              if (emit_maybe(v, __ldg(a.thf + col))) emit_exact(a, col, v, (int)id);
+            for (int e = 0; e < 4; ++e) {
+              const int j = (16 * mi + g + 8 * (e >> 1)) * FD + 8 * ni + 2 * t + (e & 1);
+              if (all_cols || j < a.D)
+                if (emit_maybe(z[mi][ni][e], __ldg(tb + j))) hit |= 1u << ((mi * NT + ni) * 4 + e);
             }
-          }
+        if (hit) {
+#pragma unroll
+          for (int mi = 0; mi < MT; ++mi)
+#pragma unroll
+            for (int ni = 0; ni < NT; ++ni)
+#pragma unroll
+              for (int e = 0; e < 4; ++e) s_scr[((mi * NT + ni) * 4 + e) * 32] = z[mi][ni][e];
+          do {
+            const int f = __ffs((int)hit) - 1;
+            hit &= hit - 1;
+            const int e = f & 3, ni = (f >> 2) % NT, mi = (f >> 2) / NT;
+            const int j = (16 * mi + g + 8 * (e >> 1)) * FD + 8 * ni + 2 * t + (e & 1);
+            emit_exact(a, r * a.D + j, s_scr[f * 32], (int)id);
+          } while (hit);
+        }
+      } else {
+#pragma unroll
+        for (int mi = 0; mi < MT; ++mi)
+#pragma unroll
+          for (int ni = 0; ni < NT; ++ni)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int j = (16 * mi + g + 8 * (e >> 1)) * FD + 8 * ni + 2 * t + (e & 1);
+              if (!all_cols && j >= a.D) continue;
+              const float v = z[mi][ni][e];
+              const int col = r * a.D + j;
+              if constexpr (MODE == PROJ_ROWS) {
+                a.out[row * (long)C + col] = v;
+              } else {  // PROJ_COLS
+                const int slot = a.col_slot ? a.col_slot[col] : col;
+                if (slot >= 0) a.out[(long)slot * a.ld_out + row] = v;
+              }
+            }
+      }
     }
   }
 }
 
 template <int FD, int MODE>
 static cudaError_t launch_tc(const ProjArgs& a, int num_sms, cudaStream_t st) {
-  const size_t smem = (size_t)a.R * 3 * (FD * FD / 32) * 4;
+  size_t smem = (((size_t)a.R * 3 * (FD * FD / 32) + 3) & ~(size_t)3) * 4;
+  if (MODE == PROJ_EMIT) smem += (size_t)4 * 32 * 32 * 4;  // 4 warps x 32 elements x 32 lanes
   cudaError_t e = cudaFuncSetAttribute(k_project_tc<FD, MODE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
