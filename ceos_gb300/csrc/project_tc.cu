@@ -65,15 +65,16 @@ CEOS_DEV uint32_t trans8x8(uint32_t x) {
 CEOS_DEV uint32_t hbits(int i, int j) { return (__popc(i & j) & 1) ? 0xBF80u : 0x3F80u; }
 CEOS_DEV uint32_t hpair(int i0, int j0, int i1, int j1) { return hbits(i0, j0) | (hbits(i1, j1) << 16); }
 
-CEOS_DEV float flip(float v, uint32_t word, int bit) {
-  return __uint_as_float(__float_as_uint(v) ^ ((((word >> bit) & 1u) ^ 1u) << 31));
+// Sign flip of an element whose (inverted) sign bit is bit k of nw.
+CEOS_DEV float flipn(float v, uint32_t nw, int k) {
+  return __uint_as_float(__float_as_uint(v) ^ ((nw << (31 - k)) & 0x80000000u));
 }
 
 }  // namespace
 
 // One warp per vector at a time; grid-strided over rows.
 template <int FD, int MODE>
-__global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
+__global__ void __launch_bounds__(128, 4) k_project_tc(ProjArgs a) {
   constexpr int F = FD * FD;
   constexpr int MT = FD / 16;  // 16-row tiles
   constexpr int NT = FD / 8;   // 8-column tiles
@@ -129,13 +130,30 @@ __global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
 #pragma unroll
         for (int ni = 0; ni < NT; ++ni)
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int j = (16 * mi + g + 8 * (e >> 1)) * FD + 8 * ni + 2 * t + (e & 1);
-            z[mi][ni][e] = j < a.d ? __ldg(xr + j) : 0.0f;
+          for (int h = 0; h < 2; ++h) {
+            // an even element pair; rows are zero padded up to ldx (a multiple
+            // of 8), so a pair starting below ldx lies inside the row
+            const int j = (16 * mi + g + 8 * h) * FD + 8 * ni + 2 * t;
+            const float2 p = j < a.ldx ? __ldg(reinterpret_cast<const float2*>(xr + j))
+                                       : make_float2(0.0f, 0.0f);
+            z[mi][ni][2 * h] = p.x;
+            z[mi][ni][2 * h + 1] = p.y;
           }
 #pragma unroll 1
       for (int round = 0; round < 3; ++round) {
         const uint32_t* sw = s_signs + ((size_t)r * 3 + round) * WORDS;
+        // The sign bits of a fragment row i = 16 mi + g + 8 h: element
+        // j = 8 ni + 2 t + c of the row has bit (i FD + j) of the round's
+        // table, all in word (i FD) >> 5 (j < FD <= 32); nw[mi][h] holds that
+        // word inverted (bit set => flip) and shifted so bit 8 ni + c is j's.
+        uint32_t nw[MT][2];
+#pragma unroll
+        for (int mi = 0; mi < MT; ++mi)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int b0 = (16 * mi + g + 8 * h) * FD;
+            nw[mi][h] = ~(sw[b0 >> 5] >> ((b0 & 31) + 2 * t));
+          }
         // A fragments of signs (.) X, split hi / lo
         uint32_t ah[MT][KT][4], al[MT][KT][4];
 #pragma unroll
@@ -147,12 +165,8 @@ __global__ void __launch_bounds__(128) k_project_tc(ProjArgs a) {
               // q: 0 = (row g, cols 2t..), 1 = (row g+8), 2 = (row g, cols +8), 3 = (row g+8, cols +8)
               const int ni = 2 * ki + (q >> 1);
               const int e0 = (q & 1) ? 2 : 0;
-              const int i = 16 * mi + g + 8 * (q & 1);
-              const int j = 8 * ni + 2 * t;
-              const int b = i * FD + j;  // element index of the first of the pair
-              const uint32_t w = sw[b >> 5];
-              const float v0 = flip(z[mi][ni][e0], w, b & 31);
-              const float v1 = flip(z[mi][ni][e0 + 1], w, (b + 1) & 31);
+              const float v0 = flipn(z[mi][ni][e0], nw[mi][q & 1], 8 * ni);
+              const float v1 = flipn(z[mi][ni][e0 + 1], nw[mi][q & 1], 8 * ni + 1);
               split2(v0, v1, ah[mi][ki][q], al[mi][ki][q]);
             }
         // Y = A . H
