@@ -792,15 +792,8 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
         for (int u = 0; u < kU; ++u) {
           const bool has = c0 + 32 * u + lane < w1;
           const int dg = has ? ((v[u].x >> shift) & (nbins - 1)) : 0;
-          // lanes with the same digit: one ballot per digit bit
-          unsigned peers = __ballot_sync(0xffffffffu, has);
-#pragma unroll
-          for (int bit = 0; bit < kPartMaxBits; ++bit) {
-            if (bit < hb) {
-              const unsigned bb = __ballot_sync(0xffffffffu, (dg >> bit) & 1);
-              peers &= ((dg >> bit) & 1) ? bb : ~bb;
-            }
-          }
+          // lanes with the same digit (lanes without a pair get a key no digit has)
+          const unsigned peers = __match_any_sync(0xffffffffu, has ? dg : nbins + lane);
           const int rank = __popc(peers & ((1u << lane) - 1u));
           const int b = has ? myh[dg] : 0;
           __syncwarp();
@@ -902,7 +895,15 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       int off = 0;
       for (int w = 0; w < warp; ++w) off += wcnt[w];
       const int cnt = wcnt[warp];
-      for (int i = lane; i < cnt; i += 32) src[off + i] = wout[i];
+      // eight loads in flight per lane (global to global)
+      for (int i0 = lane; i0 < cnt; i0 += 32 * 8) {
+        int2 tv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) tv[u] = i0 + 32 * u < cnt ? wout[i0 + 32 * u] : make_int2(0, 0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (i0 + 32 * u < cnt) src[off + i0 + 32 * u] = tv[u];
+      }
       if (threadIdx.x == 0) {
         int tot = 0;
         for (int w = 0; w < kSortWarps; ++w) tot += wcnt[w];
