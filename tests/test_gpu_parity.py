@@ -258,6 +258,39 @@ def test_exact_fallback_on_massive_ties(gpu, oracle):
     assert np.array_equal(gi, oi) and bits_equal(gv, ov)
 
 
+def test_sampled_buckets_heavy_tied_bin(gpu, oracle):
+    """50 identical high-norm rows rank first in most column ends of a
+    top_m = 100 build: their 50 equal values share one histogram bin above the
+    selection threshold, more than the per-bin insertion sort takes, so the
+    bin-ordered selection falls back to its block sort. Ties go to the
+    smaller id on both sides, so the buckets stay exact."""
+    n, d = 120000, 32
+    X = netflix_like(n, d, seed=91)
+    norms = np.linalg.norm(X, axis=1)
+    X[1000:1050] = X[7] * np.float32(3.0 * norms.max() / norms[7])  # leads 65 of 256 ends
+    g, o = build_pair(gpu, oracle, X, 64, 2, 100, 17)
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+
+
+def test_sampled_buckets_signed_zero_thresholds(gpu, oracle):
+    """Only 30 of 70,000 rows are nonzero, so every column end's top 100 ends
+    in projections of zero rows, which are +0 or -0 by the exact sign-flip and
+    butterfly arithmetic (fkey ranks -0 below +0). The sample thresholds land
+    on zero keys, where the float prefilter admits both zeros and the exact
+    key test decides. The overflowing lists take the exact fallback, and the
+    buckets match the oracle bit for bit."""
+    n, d = 70000, 24
+    X = np.zeros((n, d), np.float32)
+    rows = np.random.default_rng(93).choice(n, 30, replace=False)
+    X[rows] = netflix_like(30, d, seed=93)
+    g, o = build_pair(gpu, oracle, X, 32, 2, 100, 19)
+    gi, gv = g.buckets()
+    oi, ov = o.buckets()
+    assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+
+
 def test_recall_vs_fp64(gpu, oracle):
     n, d = 20000, 300
     X = netflix_like(n, d, seed=91)
