@@ -119,8 +119,9 @@ def run_served(idx, reqs, precision, open_loop=True):
 def served_leg(args):
     """Served queries (config of the request loop): build the 2.34M x 150 index,
     drive the open-loop stream through the server in FP32 and split-BF16, and at
-    saturation (all requests queued at once); recall@k per request against the
-    GPU FP64 ground truth on a sample of requests."""
+    saturation (all requests queued at once); then the same requests through the
+    plain FP32 path (one search call per request). recall@k per request against
+    the GPU FP64 ground truth on a sample of requests."""
     import ceos_gb300.CEOs as CEOs
     from ceos_gb300 import _capi
 
@@ -140,10 +141,8 @@ def served_leg(args):
     nsq = sum(len(r[1]) for r in sample)
     gtQ = np.concatenate([r[1] for r in sample])
     gt_ids, _ = _capi.bruteforce_fp64(X, gtQ, max(cfg["ks"]))
-    for prec in ("fp32", "split_bf16"):
-        st, res = run_served(idx, reqs, prec, open_loop=True)
-        sat, _ = run_served(idx, reqs, prec, open_loop=False)
-        # recall@min(k, 10) of the sampled requests, by n_probed_vectors
+    def recall_by_probes(res):
+        """recall@min(k, 10) of the sampled requests, by n_probed_vectors"""
         rec = {}
         row = 0
         for (t_arr, Qr, k, s), (ids, _) in zip(sample, res[:len(sample)]):
@@ -151,6 +150,11 @@ def served_leg(args):
             g = gt_ids[row:row + len(Qr), :kk]
             row += len(Qr)
             rec.setdefault(s, []).extend(len(np.intersect1d(a[:kk], b)) / kk for a, b in zip(ids, g))
+        return {str(s): float(np.mean(v)) for s, v in sorted(rec.items())}
+
+    for prec in ("fp32", "split_bf16"):
+        st, res = run_served(idx, reqs, prec, open_loop=True)
+        sat, _ = run_served(idx, reqs, prec, open_loop=False)
         out[prec] = {
             "open_loop": {"offered_req_per_s": cfg["rate"], "queries": st["queries"],
                           "requests": st["requests"], "wall_s": st["busy_s"],
@@ -160,10 +164,33 @@ def served_leg(args):
                           "graph_launches": st["graph_launches"]},
             "saturation": {"queries_per_s": sat["queries"] / sat["busy_s"], "p50_ms": sat["p50_ms"],
                            "p99_ms": sat["p99_ms"], "mean_batch_queries": sat["mean_batch_queries"]},
-            "recall_at_min_k_10_by_probes": {str(s): float(np.mean(v)) for s, v in sorted(rec.items())},
+            "recall_at_min_k_10_by_probes": recall_by_probes(res),
             "recall_queries": nsq,
         }
+    # the plain FP32 path: the same requests back to back, one search call each
+    # (host buffers in and out, no serving loop, no request batching)
     idx.precision = "fp32"
+    for t_arr, Qr, k, s in reqs[:64]:
+        idx.n_probed_vectors = s
+        idx.search_coCEOs_Est(Qr, k)
+    lat, res = [], []
+    t0 = time.perf_counter()
+    for t_arr, Qr, k, s in reqs:
+        t1 = time.perf_counter()
+        idx.n_probed_vectors = s
+        res.append(idx.search_coCEOs_Est(Qr, k))
+        lat.append(time.perf_counter() - t1)
+    wall = time.perf_counter() - t0
+    nq = sum(len(r[1]) for r in reqs)
+    out["plain_fp32"] = {"queries_per_s": nq / wall, "requests": len(reqs), "queries": nq,
+                         "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                         "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                         "recall_at_min_k_10_by_probes": recall_by_probes(res)}
+    sp, pl = out["split_bf16"], out["plain_fp32"]
+    out["served_split_vs_plain_fp32_qps"] = sp["saturation"]["queries_per_s"] / pl["queries_per_s"]
+    out["recall_gap_served_split_vs_plain_fp32"] = max(
+        abs(sp["recall_at_min_k_10_by_probes"][s] - pl["recall_at_min_k_10_by_probes"][s])
+        for s in pl["recall_at_min_k_10_by_probes"])
     return out
 
 
