@@ -42,8 +42,10 @@ bool project_tc_supported(int L);
 cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st);
 
 // ---- selection (select.cu) ----
-// Per column: u32 thresholds so that about `rank` sample values pass each end,
-// and their float prefilter bounds (thf, see ProjArgs::thf).
+// Per column of the row-major sample samp[S][C]: u32 key thresholds, the lower
+// edge of the 16-bit key prefix holding each end's rank-`rank` key (so at least
+// `rank` sampled values pass), and their float prefilter bounds (thf, see
+// ProjArgs::thf).
 cudaError_t launch_sample_thresholds(const float* samp, long S, int C, int rank, uint32_t* th,
                                      float2* thf, cudaStream_t st);
 // Per column end: top-m of the emitted candidates -> buckets; flags failures.
