@@ -111,8 +111,10 @@ struct QueryArgs {
 enum QueryMode { Q_ESTIMATE = 0, Q_UNION = 1 };
 
 cudaError_t launch_query_buckets(const QueryArgs& a, int mode, int grid, size_t smem, cudaStream_t st);
-// Sort-based coCEOs-Est search (distinct ids per column): stable radix sort of the
-// probed (id, value) pairs by id, in-order run sums, top-c, rerank, top-k.
+// Sort-based coCEOs-Est search (distinct ids per column): the probed (id, value)
+// pairs ordered by id (one stable scatter into 1024-id partitions summed in
+// per-warp shared-memory tables when ids are below 2^20, else a stable LSD radix
+// sort and run sums), every sum taken in probe order; top-c, rerank, top-k.
 cudaError_t launch_query_sorted(const QueryArgs& a, int grid, size_t smem, cudaStream_t st);
 size_t query_sorted_smem(const QueryArgs& a);
 int query_sorted_blocks_per_sm(size_t smem);
