@@ -66,3 +66,32 @@ def test_tensor_build_recall_matches_fp32(gpu, oracle):
     same = np.mean([len(np.intersect1d(a, b)) / a.size for a, b in
                     zip(b32.reshape(-1, b32.shape[-1]), bsp.reshape(-1, bsp.shape[-1]))])
     assert same > 0.98, same
+
+
+def test_tensor_sampled_build_selects_exactly(gpu):
+    """n > 65536 takes the sampled-threshold build; with the tensor-core
+    projection its buckets must be exactly the two-ended top-m of the
+    split-precision projections themselves. The dense build of the same index
+    produces the same projection values, and the order is the library's: key
+    of the value, then the smaller id."""
+    n, d, D, R, m = 70000, 150, 128, 2, 64
+    X = netflix_like(n, d, seed=17)
+    dense = gpu.CEOs(n, d)
+    dense.setIndexParam(D, R, m, 1, 23)
+    dense.precision = "split_bf16"
+    dense.build(X)
+    P = dense.projections()
+    idx = gpu.CEOs(n, d)
+    idx.setIndexParam(D, R, m, 1, 23)
+    idx.precision = "split_bf16"
+    idx.build_coCEOs_Est(X)
+    bi, bv = idx.buckets()
+    for col in range(D * R):
+        for end, vals in ((0, P[:, col]), (1, -P[:, col])):
+            u = vals.view(np.uint32).astype(np.int64)
+            key = np.where(u & 0x80000000, ~u & 0xffffffff, u | 0x80000000)
+            kth = np.partition(key, n - m)[n - m]
+            cand = np.nonzero(key >= kth)[0]
+            top = cand[np.lexsort((cand, -key[cand]))][:m]
+            assert np.array_equal(bi[col, end], top), (col, end)
+            assert np.array_equal(bv[col, end].view(np.uint32), vals[top].view(np.uint32)), (col, end)
