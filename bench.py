@@ -25,6 +25,7 @@ import ctypes.util
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -433,7 +434,10 @@ class ClockSampler:
     def __init__(self, gpu_index=0):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples (200 ms apart) go to a scratch file; the JSON line carries
+        # their summary
+        self.path = os.path.join(os.environ.get("CEOS_BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"ceos_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
