@@ -801,6 +801,16 @@ extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float*
   q.distinct_ids = 1;
   q.out_ids = d_ids;
   q.out_d = d_dists;
+  if (c.precision == CEOS_PRECISION_SPLIT_BF16) {
+    // The split form scans the bfloat16 row copy; making that copy allocates,
+    // so this entry point only uses one that an earlier search already made.
+    if (!c.xb_valid)
+      return fail(CEOS_ERR_UNSUPPORTED,
+                  "split-precision index without its bfloat16 row copy: run one allocating "
+                  "split search (ceos_search_device or a host search) first");
+    q.Xb = c.dXb.as<uint16_t>();
+    q.rescore = 4 * k;
+  }
   const long tc = table_capacity(c.s, c.p);
   if (tc < 0) return fail(CEOS_ERR_UNSUPPORTED, "n_probed_vectors * n_probed_points too large");
   q.table_cap = (int)tc;

@@ -172,6 +172,17 @@ int load_core(Core& c, uint32_t kind, long* n_points, const char* path) {
   int32_t prm[16];
   r.get(prm, sizeof(prm));
   if (!r.ok || n_rows < 1 || prm[1] < 1) return fail(CEOS_ERR_ARG, "corrupt index header");
+  // The header must describe an index of this handle's kind before anything
+  // is allocated: CEOs files hold a dense, coCEOs-Est or CEOs-Hash build with
+  // n_points == the stored row count, streamCEOs files a stream build.
+  {
+    const int b = prm[13];
+    const bool kind_ok = kind == 1u ? (b == B_DENSE || b == B_COCEOS || b == B_HASH) : (b == B_STREAM);
+    if (!kind_ok) return fail(CEOS_ERR_ARG, "corrupt index header (build kind %d)", b);
+    if (prm[14] != 0 && prm[14] != 1) return fail(CEOS_ERR_ARG, "corrupt index header (projection form %d)", prm[14]);
+    if (kind == 1u && (int64_t)prm[0] != n_rows)
+      return fail(CEOS_ERR_ARG, "corrupt index header (n_points %d, %lld rows)", prm[0], (long long)n_rows);
+  }
   *n_points = prm[0];
   c.n_features = prm[1];
   c.set_param(prm[2], prm[3], prm[4], prm[5], prm[6]);

@@ -10,7 +10,7 @@
  * Each declaration names the reference interface it replaces (NinhPham/CEOs,
  * paths relative to that project). The reference binds its classes to Python
  * through pybind11 in python/python_wrapper.cpp; the same methods map onto
- * these functions one to one (see INTEGRATION.md for the binding).
+ * these functions one to one.
  *
  * Status codes: every int-returning call returns CEOS_OK (0) or a negative
  * CEOS_ERR_* code; ceos_last_error() gives the message of the calling
@@ -93,8 +93,9 @@ int ceos_clear(ceos_index* h);
 int ceos_set_query_param(ceos_index* h, int n_probed_vectors, int n_probed_points, int n_cand);
 int ceos_get_query_param(const ceos_index* h, int* n_probed_vectors, int* n_probed_points,
                          int* n_cand);
-/* centering attribute: python/python_wrapper.cpp:35 (src/CEOs.h:55). Stored only; see
- * ceos_build_ceos_hash. */
+/* centering attribute: python/python_wrapper.cpp:35 (src/CEOs.h:55). Read by
+ * ceos_build_ceos_hash only, as in the reference: 1 = center the rows by their column means
+ * before the build. */
 int ceos_set_centering(ceos_index* h, int centering);
 int ceos_get_centering(const ceos_index* h, int* centering);
 /* CEOS_PRECISION_* for the next search (no counterpart in the reference). The split form
@@ -115,9 +116,11 @@ int ceos_build_coceos_est(ceos_index* h, const float* X);
 /* search_coCEOs_Est: python/python_wrapper.cpp:44-45 -> src/CEOs.cpp:450-694 */
 int ceos_search_coceos_est(ceos_index* h, const float* Q, int n_queries, int n_neighbors,
                            int verbose, int32_t* ids, float* dists);
-/* build_CEOs_Hash: python/python_wrapper.cpp:46 -> src/CEOs.cpp:708-840. The reference's
- * centering branch (src/CEOs.cpp:721-728) subtracts an n-vector of row means and is not
- * well defined; the flag is accepted and ignored. */
+/* build_CEOs_Hash: python/python_wrapper.cpp:46 -> src/CEOs.cpp:708-840. With centering set,
+ * the rows are centered by their column means (double sums in a fixed order) and the index,
+ * its rerank and its scores use the centered rows. The reference's branch
+ * (src/CEOs.cpp:721-728) subtracts an n-vector of row means from d-vectors, which is not a
+ * column centering; this opt-in form is the corrected one. */
 int ceos_build_ceos_hash(ceos_index* h, const float* X);
 /* search_CEOs_Hash: python/python_wrapper.cpp:47-48 -> src/CEOs.cpp:850-1066 (n_cand unused,
  * as in the reference). */
@@ -135,6 +138,13 @@ int ceos_search_device(ceos_index* h, int algo, const float* d_Q, int n_queries,
  * allocation could stall the device or fail mid-request. Same arguments and results as
  * ceos_search_device(h, CEOS_ALGO_COCEOS, ...), but asynchronous: the results are valid once
  * `cuda_stream` (NULL = the index's stream) has been synchronized.
+ * It always runs the hash-table query kernel (the allocating search may pick the sorted one;
+ * both sum every estimate in the same order, so the results are the same), and rejects with
+ * CEOS_ERR_UNSUPPORTED an n_probed_vectors * n_probed_points beyond that kernel's table
+ * capacity. On a split-precision index it needs the bfloat16 row copy, which the first
+ * allocating split search makes: before that copy exists it returns CEOS_ERR_UNSUPPORTED;
+ * afterwards it scans in bfloat16 and rescores the best 4 * n_neighbors in FP32, as
+ * ceos_search_device does.
  * Scratch (padded queries, their projections, and per-CTA hash tables when a table does not
  * fit in shared memory) comes from one fixed 64 MiB device array that every GPU loading the
  * library holds until exit. A batch needing more than that is rejected with

@@ -9,8 +9,10 @@ of a request. Its scratch comes from one fixed device array instead.
 Checked through the C ABI against the allocating device search
 (ceos_search_device), on two calls in a row - the second call finds the
 array holding the first call's contents - for a query table that fits in
-shared memory and for one that lives in the scratch array; and a batch larger
-than the array is refused. This file is collected last on purpose.
+shared memory, for one that lives in the scratch array, and for a
+split-precision index (bfloat16 scan, FP32 rescore); a batch larger than the
+array is refused, and so is a split-precision index whose bfloat16 row copy
+does not exist yet. This file is collected last on purpose.
 """
 import ctypes as C
 import ctypes.util
@@ -118,5 +120,47 @@ def test_noalloc_rejects_oversized_batch(gpu):
         _capi.check(L.ceos_search_coceos_est_device_noalloc(idx._h, C.c_void_p(dQ), 100, k,
                                                             C.c_void_p(dI), C.c_void_p(dD), None))
         rt.sync()
+    finally:
+        rt.free_all()
+
+
+def test_noalloc_split_precision(gpu):
+    """On a split-precision index the allocation-free search scans the bfloat16
+    row copy and rescores the best 4k in FP32, like ceos_search_device. The copy
+    is made by the first allocating split search; before that the entry point
+    refuses rather than allocate it or fall back to a plain FP32 rerank."""
+    from ceos_gb300 import _capi
+
+    L = _capi.lib()
+    n, d, k = 6000, 256, 10
+    X = netflix_like(n, d, seed=11)
+    Q = gaussian_queries(40, d, seed=12)
+    nq = Q.shape[0]
+    idx = gpu.CEOs(n, d)
+    idx.setIndexParam(256, 2, 100, 1, 42)
+    idx.precision = "split_bf16"
+    idx.build_coCEOs_Est(X)
+    idx.n_probed_vectors, idx.n_cand = 20, 500
+    rt = _Cudart()
+    try:
+        dQ = rt.put(Q)
+        dI, dD = rt.alloc(nq * k * 4), rt.alloc(nq * k * 4)
+        dI2, dD2 = rt.alloc(nq * k * 4), rt.alloc(nq * k * 4)
+        st = L.ceos_search_coceos_est_device_noalloc(idx._h, C.c_void_p(dQ), nq, k,
+                                                     C.c_void_p(dI2), C.c_void_p(dD2), None)
+        assert st == _capi.ERR_UNSUPPORTED
+        assert "bfloat16" in _capi.last_error()
+        _capi.check(L.ceos_search_device(idx._h, _capi.ALGO_COCEOS, C.c_void_p(dQ), nq, k,
+                                         C.c_void_p(dI), C.c_void_p(dD), None))
+        ref_i = rt.get(dI, (nq, k), np.int32)
+        ref_d = rt.get(dD, (nq, k), np.float32)
+        for _ in range(2):
+            _capi.check(L.ceos_search_coceos_est_device_noalloc(
+                idx._h, C.c_void_p(dQ), nq, k, C.c_void_p(dI2), C.c_void_p(dD2), None))
+            rt.sync()
+            got_i = rt.get(dI2, (nq, k), np.int32)
+            got_d = rt.get(dD2, (nq, k), np.float32)
+            assert np.array_equal(got_i, ref_i)
+            assert np.array_equal(got_d.view(np.uint32), ref_d.view(np.uint32))
     finally:
         rt.free_all()
