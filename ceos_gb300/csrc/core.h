@@ -568,8 +568,12 @@ struct Core {
 
   // Estimate searches run sorted (k_query_sorted) unless the hash table fits
   // in shared memory with two CTAs per SM; CEOS_GB300_QUERY=table|sorted
-  // forces one form.
+  // forces one form for indexes whose columns hold distinct ids.
   bool use_sorted(const QueryArgs& q) const {
+    // A FIFO stream's stale bucket rows can repeat an id within one column.
+    // Only the sorted kernel adds such repeats in entry order (the table's
+    // shared adds would apply them in hardware order), so it always runs.
+    if (!q.distinct_ids) return true;
     const char* e = std::getenv("CEOS_GB300_QUERY");
     if (e && std::strcmp(e, "table") == 0) return false;
     if (e && std::strcmp(e, "sorted") == 0) return true;

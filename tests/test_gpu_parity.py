@@ -103,20 +103,6 @@ def test_coceos_search_exact(gpu, oracle, dist, n, d, D, R, m, s, c, k):
     assert np.array_equal(gi, oi) and bits_equal(gd, od)
 
 
-def test_golden_fixture(gpu):
-    f = np.load(os.path.join(GOLD, "search_small.npz"))
-    D, R, m, s, c, k, seed = [int(v) for v in f["params"]]
-    X, Q = f["X"], f["Q"]
-    g = gpu.CEOs(*X.shape)
-    g.setIndexParam(D, R, m, 1, seed)
-    g.build_coCEOs_Est(X)
-    bi, bv = g.buckets()
-    assert np.array_equal(bi, f["bucket_ids"]) and bits_equal(bv, f["bucket_vals"])
-    g.n_probed_vectors, g.n_cand = s, c
-    ids, dists = g.search_coCEOs_Est(Q, k)
-    assert np.array_equal(ids, f["ids"]) and bits_equal(dists, f["dists"])
-
-
 def test_dense_search_exact(gpu, oracle):
     n, d = 3000, 300
     X = netflix_like(n, d, seed=21)
@@ -184,6 +170,35 @@ def test_stream_stale_rows_quirk(gpu, oracle):
     gi, gv = g.buckets()
     oi, ov = o.buckets()
     assert np.array_equal(gi, oi) and bits_equal(gv, ov)
+
+
+def test_stream_fifo_repeated_ids_exact(gpu, oracle):
+    """FIFO stale tail rows (src/streamCEOs.cpp:331-352) can repeat a live id
+    inside one column; the reference adds the repeats in entry order
+    (src/streamCEOs.cpp:489-526). With s*p small enough that the hash-table
+    kernel would be picked, every run must equal the oracle bit for bit."""
+    d = 16
+    X = netflix_like(400, d, seed=51)
+    Q = gaussian_queries(64, d, seed=52)
+    g, o = gpu.streamCEOs(d), oracle.streamCEOs(d)
+    for s in (g, o):
+        s.setIndexParam(32, 1, 30, 1, 3)
+        s.build(X[:200])
+        s.update(X[200:215], 180)
+        s.update(X[215:230], 5)
+        s.n_probed_vectors, s.n_probed_points, s.n_cand = 8, 30, 40
+    gi, _ = g.buckets()
+    live = g.size
+    # the setup must hold a column end in which a live id appears twice
+    rep = 0
+    for col in gi.reshape(-1, gi.shape[-1]):
+        ids = col[(col >= 0) & (col < live)]
+        rep += len(ids) - len(np.unique(ids))
+    assert rep > 0
+    bi, bd = o.estimate_search(Q, 10)
+    for _ in range(10):
+        ai, ad = g.estimate_search(Q, 10)
+        assert np.array_equal(ai, bi) and bits_equal(ad, bd)
 
 
 def test_edge_cases(gpu, oracle):
