@@ -32,8 +32,10 @@
 //    multiply-add chains over float4 chunks, then a butterfly; see dot_fma),
 //    the one the GPU kernels compute. The reference uses Eigen's vectorised
 //    dot, whose association differs at the ulp level.
-//  * Per-query estimates are kept in an ordered map instead of tsl::robin_map;
-//    the accumulation order per point (probe pop order) is the reference's.
+//  * Per-query estimates are kept in an open-addressing table of this file
+//    (EstTable) instead of tsl::robin_map; the accumulation order per point
+//    (probe pop order) is the reference's, and the total order above makes
+//    the candidate selection independent of the table's iteration order.
 //  * Parameter errors return a negative status instead of exit(1); asking for
 //    more candidates than exist uses all of them instead of popping an empty
 //    heap (src/CEOs.cpp:634-647 is undefined behaviour there).
@@ -45,16 +47,19 @@
 //
 // Pins: the FWHT is checked bit for bit against the reference's own FFHT
 // sources compiled by oracle/Makefile (target `ref`), and the sign generator
-// against std::default_random_engine and a known-answer vector. The rest of the
-// reference (Eigen and Boost are not available) could not be compiled, so the
-// search/selection logic is a restatement without a reference run to pin it.
+// against std::default_random_engine and a known-answer vector. The whole
+// index path is checked against the reference's own CEOs / streamCEOs classes,
+// compiled unchanged by the same Makefile against stand-ins for the Eigen and
+// Boost headers (oracle/refshim): bucket values bit-identical, bucket ids
+// equal up to the order of exact ties, search ids equal and scores within
+// 1e-5 relative (tests/test_reference_pins.py, golden fixtures made by
+// tests/golden/make_reference_golden.py).
 
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
-#include <map>
 #include <queue>
 #include <random>
 #include <vector>
@@ -101,6 +106,49 @@ struct WorstOnTop {
   bool operator()(const Item& a, const Item& b) const { return better(a, b); }
 };
 using MinQue = std::priority_queue<Item, std::vector<Item>, WorstOnTop>;
+
+// Per-query estimate accumulator: open addressing with linear probing over a
+// power-of-two table sized for the number of probed pairs. add() keeps the
+// first value of an id as is and adds later ones in call order, which is the
+// reference's per-point accumulation (src/CEOs.cpp:562-610).
+struct EstTable {
+  std::vector<int> keys;
+  std::vector<float> vals;
+  std::vector<int> used;  // occupied slots, in first-insertion order
+  unsigned mask = 0;
+  void reset(size_t expected) {
+    size_t cap = 16;
+    while (cap < 2 * expected + 16) cap <<= 1;
+    if (keys.size() != cap) {
+      keys.assign(cap, -1);
+      vals.assign(cap, 0.0f);
+    } else {
+      for (int sl : used) keys[sl] = -1;
+    }
+    used.clear();
+    mask = (unsigned)cap - 1;
+  }
+  void add(int id, float v) {
+    unsigned h = ((unsigned)id * 2654435761u) & mask;
+    while (true) {
+      if (keys[h] == id) {
+        vals[h] += v;
+        return;
+      }
+      if (keys[h] == -1) {
+        keys[h] = id;
+        vals[h] = v;
+        used.push_back((int)h);
+        return;
+      }
+      h = (h + 1) & mask;
+    }
+  }
+  template <typename F>
+  void for_each(F f) const {
+    for (int sl : used) f(keys[sl], vals[sl]);
+  }
+};
 
 // Bounded insertion used by every top-K loop of the reference
 // (e.g. src/CEOs.cpp:393-399): push while not full, else replace the worst if
@@ -267,6 +315,48 @@ static void select_column(const float* col_vals, long n, long stride, int m,
     ids_far[r] = far.top().id;
     vals_far[r] = far.top().val;
     far.pop();
+  }
+}
+
+// Two-ended top-m of every projection column of n rows, laid out as
+// select_column writes them ([C][2][m] ids and values). The rows are
+// projected in chunks, so only chunk x C projections exist at a time (the
+// reference holds the whole n x C matrix, src/CEOs.cpp:335); each column's
+// heaps take the rows in ascending order, as select_column's do, so the
+// buckets are the same.
+static void select_all_columns(const float* X, long n, int d, int F, int D, int R,
+                               const uint8_t* bits, int m, int* B_ids, float* B_vals) {
+  const int C = D * R;
+  const long chunk = 2048;
+  const int cb = 16;  // columns per task: one 64-byte line of a projected row
+  std::vector<MinQue> close(C), far(C);
+  std::vector<float> P((size_t)std::min<long>(chunk, std::max<long>(n, 1)) * C);
+  for (long r0 = 0; r0 < n; r0 += chunk) {
+    const long nr = std::min(chunk, n - r0);
+    project_rows(X + (size_t)r0 * d, nr, d, F, D, R, bits, P.data());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int c0 = 0; c0 < C; c0 += cb) {
+      const int c1 = std::min(C, c0 + cb);
+      for (long i = 0; i < nr; ++i) {
+        const float* row = P.data() + (size_t)i * C;
+        for (int c = c0; c < c1; ++c) {
+          offer(close[c], m, (int)(r0 + i), row[c]);
+          offer(far[c], m, (int)(r0 + i), -row[c]);
+        }
+      }
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int c = 0; c < C; ++c) {
+    const size_t o = (size_t)c * 2 * m;
+    for (int r = m - 1; r >= 0; --r) {
+      B_ids[o + r] = close[c].top().id;
+      B_vals[o + r] = close[c].top().val;
+      close[c].pop();
+      B_ids[o + m + r] = far[c].top().id;
+      B_vals[o + m + r] = far[c].top().val;
+      far[c].pop();
+    }
   }
 }
 
@@ -444,16 +534,10 @@ struct OracleCEOs {
     common_build(Xin);
     if (!with_vals && centering) center_rows();
     const int Cc = C();
-    std::vector<float> Pt((size_t)n_points * Cc);
-    project_rows(X.data(), n_points, n_features, fhtDim, n_proj, n_repeats, bits.data(), Pt.data());
     B_ids.assign((size_t)Cc * 2 * top_m, 0);
     B_vals.assign((size_t)Cc * 2 * top_m, 0.0f);
-#pragma omp parallel for schedule(dynamic, 4)
-    for (int c = 0; c < Cc; ++c) {
-      size_t o = (size_t)c * 2 * top_m;
-      select_column(Pt.data() + c, n_points, Cc, top_m, &B_ids[o], &B_vals[o],
-                    &B_ids[o + top_m], &B_vals[o + top_m]);
-    }
+    select_all_columns(X.data(), n_points, n_features, fhtDim, n_proj, n_repeats, bits.data(), top_m,
+                       B_ids.data(), B_vals.data());
     if (!with_vals) B_vals.assign(B_vals.size(), 0.0f);
     built = with_vals ? 2 : 3;
     return ST_OK;
@@ -513,25 +597,20 @@ struct OracleCEOs {
     {
       std::vector<float> proj, tmp, rot;
       std::vector<int> probes;
+      EstTable est;
 #pragma omp for schedule(dynamic, 1)
       for (int q = 0; q < nq; ++q) {
         const float* qv = Q + (size_t)q * d;
         project_query(qv, proj, tmp, rot);
         probe_columns(proj.data(), Cc, n_probed_vectors, probes);
-        std::map<int, float> est;
+        est.reset(probes.size() * (size_t)std::max(p, 0));
         for (int tag : probes) {
           int c = tag < 0 ? -tag - 1 : tag - 1;
           size_t o = (size_t)c * 2 * m + (tag < 0 ? m : 0);
-          for (int j = 0; j < p; ++j) {
-            int id = B_ids[o + j];
-            float v = B_vals[o + j];
-            auto it = est.find(id);
-            if (it == est.end()) est[id] = v;
-            else it->second += v;
-          }
+          for (int j = 0; j < p; ++j) est.add(B_ids[o + j], B_vals[o + j]);
         }
         MinQue cand;
-        for (auto& kv : est) offer(cand, n_cand, kv.first, kv.second);
+        est.for_each([&](int id, float v) { offer(cand, n_cand, id, v); });
         std::vector<int> cids;
         while (!cand.empty()) {
           cids.push_back(cand.top().id);
@@ -608,16 +687,10 @@ struct OracleStream {
     const int n = (int)X.size(), Cc = C();
     std::vector<float> flat((size_t)n * n_features);
     for (int i = 0; i < n; ++i) std::memcpy(&flat[(size_t)i * n_features], X[i].data(), n_features * sizeof(float));
-    std::vector<float> Pt((size_t)n * Cc);
-    project_rows(flat.data(), n, n_features, fhtDim, n_proj, n_repeats, bits.data(), Pt.data());
     B_ids.assign((size_t)Cc * 2 * top_m, 0);
     B_vals.assign((size_t)Cc * 2 * top_m, 0.0f);
-#pragma omp parallel for schedule(dynamic, 4)
-    for (int c = 0; c < Cc; ++c) {
-      size_t o = (size_t)c * 2 * top_m;
-      select_column(Pt.data() + c, n, Cc, top_m, &B_ids[o], &B_vals[o], &B_ids[o + top_m],
-                    &B_vals[o + top_m]);
-    }
+    select_all_columns(flat.data(), n, n_features, fhtDim, n_proj, n_repeats, bits.data(), top_m,
+                       B_ids.data(), B_vals.data());
     n_points = n;
   }
 
@@ -664,16 +737,10 @@ struct OracleStream {
     const int Cc = C();
     std::vector<float> flat((size_t)n * n_features);
     std::memcpy(flat.data(), Xin, flat.size() * sizeof(float));
-    std::vector<float> Pt((size_t)n * Cc);
-    project_rows(flat.data(), n, n_features, fhtDim, n_proj, n_repeats, bits.data(), Pt.data());
     B_ids.assign((size_t)Cc * 2 * top_m, 0);
     B_vals.assign((size_t)Cc * 2 * top_m, 0.0f);
-#pragma omp parallel for schedule(dynamic, 4)
-    for (int c = 0; c < Cc; ++c) {
-      size_t o = (size_t)c * 2 * top_m;
-      select_column(Pt.data() + c, n, Cc, top_m, &B_ids[o], &B_vals[o], &B_ids[o + top_m],
-                    &B_vals[o + top_m]);
-    }
+    select_all_columns(flat.data(), n, n_features, fhtDim, n_proj, n_repeats, bits.data(), top_m,
+                       B_ids.data(), B_vals.data());
     built = true;
     return ST_OK;
   }
@@ -751,12 +818,13 @@ struct OracleStream {
     {
       std::vector<float> proj, tmp, rot;
       std::vector<int> probes;
+      EstTable est;
 #pragma omp for schedule(dynamic, 1)
       for (int q = 0; q < nq; ++q) {
         const float* qv = Q + (size_t)q * d;
         project_query(qv, proj, tmp, rot);
         probe_columns(proj.data(), C(), n_probed_vectors, probes);
-        std::map<int, float> est;
+        est.reset(probes.size() * (size_t)std::max(p, 0));
         for (int tag : probes) {
           int c = tag < 0 ? -tag - 1 : tag - 1;
           size_t o = (size_t)c * 2 * m + (tag < 0 ? m : 0);
@@ -766,14 +834,11 @@ struct OracleStream {
             // the reference then reads deque_X out of range (undefined
             // behaviour). Such entries are skipped.
             if (id < 0 || id >= n_points) continue;
-            float v = B_vals[o + j];
-            auto it = est.find(id);
-            if (it == est.end()) est[id] = v;
-            else it->second += v;
+            est.add(id, B_vals[o + j]);
           }
         }
         MinQue cand;
-        for (auto& kv : est) offer(cand, n_cand, kv.first, kv.second);
+        est.for_each([&](int id, float v) { offer(cand, n_cand, id, v); });
         std::vector<int> cids;
         while (!cand.empty()) {
           cids.push_back(cand.top().id);

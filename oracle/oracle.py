@@ -21,9 +21,13 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle.so")
+# The same source built like the reference's own release build (-O3 with the
+# host's native instruction set, fused multiply-adds allowed): the timed CPU
+# baseline. liboracle.so stays the bit-exact checker.
+_TIMED_PATH = os.path.join(_HERE, "liboracle_timed.so")
 _REF_FFHT = os.path.join(_HERE, "_ref", "libffht_ref.so")
 _lock = threading.Lock()
-_lib = None
+_libs = {}
 
 _F32P = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _F64P = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -40,34 +44,43 @@ ST_MESSAGES = {
 }
 
 
-def build(force: bool = False) -> str:
-    """Compile liboracle.so with the committed Makefile (g++, OpenMP)."""
+def build(force: bool = False, timed: bool = False) -> str:
+    """Compile liboracle.so (or, with timed, liboracle_timed.so) with the
+    committed Makefile (g++, OpenMP)."""
     src = os.path.join(_HERE, "ceos_oracle.cpp")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
-        subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
-    return _LIB_PATH
+    path = _TIMED_PATH if timed else _LIB_PATH
+    if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, os.path.basename(path)], check=True)
+    return path
+
+
+def reference_root() -> str:
+    """Root of the reference project's sources (the directory holding src/):
+    $CEOS_REFERENCE, else where this build environment mounts it."""
+    return os.environ.get("CEOS_REFERENCE", "/root/reference")
 
 
 def build_ref() -> str | None:
-    """Compile the reference's FFHT (x86 only) into oracle/_ref when the
-    reference sources are present; returns the path or None."""
-    if os.path.exists(_REF_FFHT):
+    """Compile the reference's FFHT and index classes (x86 only) into
+    oracle/_ref when the reference sources are present; returns the FFHT
+    library's path or None."""
+    if os.path.exists(_REF_FFHT) and os.path.exists(os.path.join(_HERE, "_ref", "libceos_ref.so")):
         return _REF_FFHT
-    if not os.path.isdir("/root/reference/src") or os.uname().machine not in ("x86_64", "AMD64"):
-        return None
+    root = reference_root()
+    if not os.path.isdir(os.path.join(root, "src")) or os.uname().machine not in ("x86_64", "AMD64"):
+        return _REF_FFHT if os.path.exists(_REF_FFHT) else None
     try:
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True, capture_output=True)
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"CEOS_REFERENCE={root}"], check=True,
+                       capture_output=True)
     except (subprocess.CalledProcessError, FileNotFoundError):
         return None
     return _REF_FFHT if os.path.exists(_REF_FFHT) else None
 
 
-def lib():
-    global _lib
+def lib(timed: bool = False):
     with _lock:
-        if _lib is None:
-            build()
-            L = C.CDLL(_LIB_PATH)
+        if timed not in _libs:
+            L = C.CDLL(build(timed=timed))
             vp = C.c_void_p
             L.orc_sign_bits.argtypes = [C.c_int, C.c_int, _U8P]
             L.orc_sign_bits_std.argtypes = [C.c_int, C.c_int, _U8P]
@@ -123,8 +136,8 @@ def lib():
             L.orc_stream_set_exact.argtypes = [vp, C.c_int]
             L.orc_stream_set_exact.restype = None
             L.orc_stream_delete.argtypes = [vp, _I32P, C.c_int]
-            _lib = L
-    return _lib
+            _libs[timed] = L
+    return _libs[timed]
 
 
 def _check(st: int) -> None:
@@ -257,10 +270,11 @@ class _Attrs:
 
 
 class CEOs(_Attrs):
-    """Oracle twin of the reference's ``CEOs.CEOs`` (src/CEOs.h:18-114)."""
+    """Oracle twin of the reference's ``CEOs.CEOs`` (src/CEOs.h:18-114).
+    timed=True runs the natively optimised build of the same source."""
 
-    def __init__(self, n_points: int, n_features: int):
-        L = lib()
+    def __init__(self, n_points: int, n_features: int, timed: bool = False):
+        L = lib(timed)
         self._L = L
         self._h = L.orc_ceos_create(int(n_points), int(n_features))
         self._get_q = L.orc_ceos_get_query
@@ -343,10 +357,11 @@ class CEOs(_Attrs):
 
 
 class streamCEOs(_Attrs):
-    """Oracle twin of the reference's ``CEOs.streamCEOs`` (src/streamCEOs.h)."""
+    """Oracle twin of the reference's ``CEOs.streamCEOs`` (src/streamCEOs.h).
+    timed=True runs the natively optimised build of the same source."""
 
-    def __init__(self, n_features: int):
-        L = lib()
+    def __init__(self, n_features: int, timed: bool = False):
+        L = lib(timed)
         self._L = L
         self._h = L.orc_stream_create(int(n_features))
         self._get_q = L.orc_stream_get_query

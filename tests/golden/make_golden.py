@@ -1,6 +1,7 @@
 """Generate the committed golden fixtures under tests/golden/.
 
-Run in a container that has the reference sources at /root/reference (x86):
+Run where the reference sources are (CEOS_REFERENCE, default /root/reference;
+x86, because FFHT is x86 inline assembly):
 
     python tests/golden/make_golden.py
 
@@ -10,9 +11,9 @@ Run in a container that has the reference sources at /root/reference (x86):
 * fwht_ref.npz     - inputs and outputs of the reference's own FFHT
                      fht_float (src/fht.c, compiled from the reference sources
                      by oracle/Makefile target `ref`) for log_n = 1..12.
-* search_small.npz - a small end-to-end case (data, queries, parameters) with
-                     the oracle's buckets and search results, used to check
-                     the GPU library against committed vectors.
+
+The fixtures made by the reference's own index classes are written by
+make_reference_golden.py.
 """
 import json
 import os
@@ -47,21 +48,6 @@ def main():
         arrays[f"y{L}"] = y
     np.savez_compressed(os.path.join(HERE, "fwht_ref.npz"), **arrays)
 
-    # small end-to-end case (config-0 distribution, reduced size)
-    n, d, nq = 900, 44, 40
-    X = (rng.standard_normal((n, d)) / np.sqrt(d) * rng.lognormal(0, 0.5, (n, 1))).astype(np.float32)
-    Q = rng.standard_normal((nq, d)).astype(np.float32)
-    D, R, m, s, c, k, seed = 128, 2, 50, 10, 80, 10, 42
-    idx = O.CEOs(n, d)
-    idx.setIndexParam(D, R, m, 4, seed)
-    idx.build_coCEOs_Est(X)
-    idx.n_probed_vectors = s
-    idx.n_cand = c
-    ids, dists = idx.search_coCEOs_Est(Q, k)
-    bids, bvals = idx.buckets()
-    np.savez_compressed(os.path.join(HERE, "search_small.npz"), X=X, Q=Q,
-                        params=np.array([D, R, m, s, c, k, seed], np.int32),
-                        bucket_ids=bids, bucket_vals=bvals, ids=ids, dists=dists)
     print("wrote fixtures to", HERE)
 
 
