@@ -145,9 +145,61 @@ CEOS_DEV void rerank_bf16_inplace(uint64_t* keys, int n, const float* qv, int ld
   }
 }
 
+// dot_g8 of one query with two rows at once (each row's sum in exactly
+// dot_g8's order): an 8-lane group keeps twice as many loads in flight.
+CEOS_DEV void dot_g8_2(const float* __restrict__ q, const float* __restrict__ xa,
+                       const float* __restrict__ xb, int n4, int g, float& sa, float& sb) {
+  const float4* a4 = reinterpret_cast<const float4*>(xa);
+  const float4* b4 = reinterpret_cast<const float4*>(xb);
+  const float4* q4 = reinterpret_cast<const float4*>(q);
+  float s0 = 0.0f, s1 = 0.0f;
+  int c = g;
+  for (; c + 24 < n4; c += 32) {
+    float4 va[4], vb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      va[u] = __ldcg(a4 + c + 8 * u);
+      vb[u] = __ldcg(b4 + c + 8 * u);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float4 qv = q4[c + 8 * u];
+      s0 = __fmaf_rn(qv.x, va[u].x, s0);
+      s0 = __fmaf_rn(qv.y, va[u].y, s0);
+      s0 = __fmaf_rn(qv.z, va[u].z, s0);
+      s0 = __fmaf_rn(qv.w, va[u].w, s0);
+      s1 = __fmaf_rn(qv.x, vb[u].x, s1);
+      s1 = __fmaf_rn(qv.y, vb[u].y, s1);
+      s1 = __fmaf_rn(qv.z, vb[u].z, s1);
+      s1 = __fmaf_rn(qv.w, vb[u].w, s1);
+    }
+  }
+  for (; c < n4; c += 8) {
+    const float4 va = __ldcg(a4 + c), vb = __ldcg(b4 + c);
+    const float4 qv = q4[c];
+    s0 = __fmaf_rn(qv.x, va.x, s0);
+    s0 = __fmaf_rn(qv.y, va.y, s0);
+    s0 = __fmaf_rn(qv.z, va.z, s0);
+    s0 = __fmaf_rn(qv.w, va.w, s0);
+    s1 = __fmaf_rn(qv.x, vb.x, s1);
+    s1 = __fmaf_rn(qv.y, vb.y, s1);
+    s1 = __fmaf_rn(qv.z, vb.z, s1);
+    s1 = __fmaf_rn(qv.w, vb.w, s1);
+  }
+  s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, 4);
+  s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, 4);
+  s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, 2);
+  s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, 2);
+  s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, 1);
+  s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, 1);
+  sa = s0;
+  sb = s1;
+}
+
 // Rerank keys[0..n) in place: each holds a candidate id (packed key); it is
-// replaced by pack_key(<q, x_id>, id). Each warp scores four rows at a time,
-// one per 8-lane group.
+// replaced by pack_key(<q, x_id>, id). Each warp scores eight rows at a time,
+// two per 8-lane group. A slot past n re-reads the last candidate's row (its
+// loads must stay global-memory loads of a real row; the result is dropped).
 template <typename RowPtr>
 CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, RowPtr row) {
   const int lane = threadIdx.x & 31;
@@ -156,12 +208,17 @@ CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, Ro
   const int warp = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   const int n4 = ldx >> 2;
-  for (int base = warp * 4; base < n; base += nw * 4) {
-    const int i = base + grp;
-    const bool active = i < n;
-    const int id = active ? key_id(keys[i]) : 0;
-    const float d = dot_g8(qv, active ? row(id) : qv, n4, g, active);
-    if (active && g == 0) keys[i] = pack_key(d, id);
+  for (int base = warp * 8; base < n; base += nw * 8) {
+    const int i0 = base + grp, i1 = base + 4 + grp;
+    const bool a0 = i0 < n, a1 = i1 < n;
+    const int id0 = key_id(keys[a0 ? i0 : n - 1]);
+    const int id1 = key_id(keys[a1 ? i1 : n - 1]);
+    float d0, d1;
+    dot_g8_2(qv, row(id0), row(id1), n4, g, d0, d1);
+    if (g == 0) {
+      if (a0) keys[i0] = pack_key(d0, id0);
+      if (a1) keys[i1] = pack_key(d1, id1);
+    }
   }
 }
 
@@ -695,10 +752,15 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
     }
     __syncthreads();
-    // ---- 2. gather the probed pairs in probe order ----
+    // ---- 2. digit counts of the probed pairs ----
+    // Pair t = j * p + e is entry e of the j-th probed column (probe order).
+    // Warp w owns the probed columns [jw0, jw1), a contiguous run of pairs;
+    // it counts its run's first-pass digits, and the first scatter pass below
+    // reads the same run straight from the bucket table (no gathered copy).
     const int E = ns * a.p;
     constexpr int kU = 8;  // independent loads in flight per thread in every pass
     const int seg = (E + kSortWarps - 1) / kSortWarps;
+    const int jw0 = (int)((long)warp * ns / kSortWarps), jw1 = (int)((long)(warp + 1) * ns / kSortWarps);
     // partitioned accumulation: digit = id >> tb (hb bits); else 8-bit LSD digits
     const bool part = a.id_bits <= kPartIdBits;
     const int tb = min(a.id_bits, kPartTableBits);
@@ -708,30 +770,33 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     for (int i = threadIdx.x; i < (part ? kSortWarps * nbins : 2 * kSortWarps * kRadixBins); i += blockDim.x)
       rh_all[i] = 0;
     __syncthreads();
-    for (int t0 = threadIdx.x; t0 < E; t0 += kU * blockDim.x) {
-      int id[kU];
-      float v[kU];
+    auto column = [&](int j, const int*& bid, const float*& bval) {
+      const int tag = probes[j];
+      const int col = (tag < 0 ? -tag : tag) - 1;
+      const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m;
+      bid = a.bids + base;
+      bval = a.bvals + base;
+    };
+    {
+      int* myh0 = rh_all + warp * nbins;
+      for (int j = jw0; j < jw1; ++j) {
+        const int* bid;
+        const float* bval;
+        column(j, bid, bval);
+        for (int e0 = 0; e0 < a.p; e0 += 32 * kU) {
+          int id[kU];
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int t = t0 + u * blockDim.x;
-        id[u] = npts;
-        v[u] = 0.0f;
-        if (t < E) {
-          const int j = t / a.p, e = t - j * a.p;
-          const int tag = probes[j];
-          const int col = (tag < 0 ? -tag : tag) - 1;
-          const long base = (2L * col + (tag < 0 ? 1 : 0)) * a.m + e;
-          id[u] = __ldg(a.bids + base);
-          v[u] = __ldg(a.bvals + base);
-        }
-      }
+          for (int u = 0; u < kU; ++u) {
+            const int e = e0 + 32 * u + lane;
+            id[u] = e < a.p ? __ldg(bid + e) : 0;
+          }
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const int t = t0 + u * blockDim.x;
-        if (t < E) {
-          const int i = (unsigned)id[u] >= (unsigned)npts ? npts : id[u];  // stale row: dropped below
-          bufA[t] = make_int2(i, __float_as_int(v[u]));
-          atomicAdd(&rh_all[(t / seg) * nbins + ((i >> dshift0) & (nbins - 1))], 1);  // first pass's digits
+          for (int u = 0; u < kU; ++u) {
+            if (e0 + 32 * u + lane < a.p) {
+              const int i = (unsigned)id[u] >= (unsigned)npts ? npts : id[u];  // stale row: dropped below
+              atomicAdd(&myh0[(i >> dshift0) & (nbins - 1)], 1);
+            }
+          }
         }
       }
     }
@@ -781,29 +846,56 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
         if (part && threadIdx.x == 0) pstart[nbins] = E;
       }
       __syncthreads();
-      for (int c0 = w0; c0 < w1; c0 += 32 * kU) {
-        int2 v[kU];
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          const int i = c0 + 32 * u + lane;
-          v[u] = i < w1 ? src[i] : make_int2(0, 0);
+      // one 32-pair step: lanes with a pair are ranked among the lanes of equal
+      // digit (lanes without one get a key no digit has), in lane order
+      auto place = [&](const int2 v, const bool has) {
+        const int dg = has ? ((v.x >> shift) & (nbins - 1)) : 0;
+        const unsigned peers = __match_any_sync(0xffffffffu, has ? dg : nbins + lane);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        const int b = has ? myh[dg] : 0;
+        __syncwarp();
+        if (has) {
+          dst[b + rank] = v;
+          if (rank == 0) myh[dg] = b + __popc(peers);
+          // the next pass's digit counts, by destination segment
+          if (more) atomicAdd(&rn[((b + rank) / seg) * kRadixBins + ((v.x >> (shift + 8)) & 255)], 1);
         }
+        __syncwarp();
+      };
+      if (ps == 0) {
+        // the warp's run of probed columns, straight from the bucket table
+        for (int j = jw0; j < jw1; ++j) {
+          const int* bid;
+          const float* bval;
+          column(j, bid, bval);
+          for (int e0 = 0; e0 < a.p; e0 += 32 * kU) {
+            int2 v[kU];
 #pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          const bool has = c0 + 32 * u + lane < w1;
-          const int dg = has ? ((v[u].x >> shift) & (nbins - 1)) : 0;
-          // lanes with the same digit (lanes without a pair get a key no digit has)
-          const unsigned peers = __match_any_sync(0xffffffffu, has ? dg : nbins + lane);
-          const int rank = __popc(peers & ((1u << lane) - 1u));
-          const int b = has ? myh[dg] : 0;
-          __syncwarp();
-          if (has) {
-            dst[b + rank] = v[u];
-            if (rank == 0) myh[dg] = b + __popc(peers);
-            // the next pass's digit counts, by destination segment
-            if (more) atomicAdd(&rn[((b + rank) / seg) * kRadixBins + ((v[u].x >> (shift + 8)) & 255)], 1);
+            for (int u = 0; u < kU; ++u) {
+              const int e = e0 + 32 * u + lane;
+              v[u] = make_int2(0, 0);
+              if (e < a.p) {
+                const int id = __ldg(bid + e);
+                v[u] = make_int2((unsigned)id >= (unsigned)npts ? npts : id, __float_as_int(__ldg(bval + e)));
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+              if (e0 + 32 * u >= a.p) break;
+              place(v[u], e0 + 32 * u + lane < a.p);
+            }
           }
-          __syncwarp();
+        }
+      } else {
+        for (int c0 = w0; c0 < w1; c0 += 32 * kU) {
+          int2 v[kU];
+#pragma unroll
+          for (int u = 0; u < kU; ++u) {
+            const int i = c0 + 32 * u + lane;
+            v[u] = i < w1 ? src[i] : make_int2(0, 0);
+          }
+#pragma unroll
+          for (int u = 0; u < kU; ++u) place(v[u], c0 + 32 * u + lane < w1);
         }
       }
       __syncthreads();
@@ -890,28 +982,16 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
         const int ct = tag[loc];
         if (ct != 0) emit(ct, loc, tab[loc]);
       }
+      __syncwarp();
+      // the warp's sums fill dst[e0, e0 + cnt); the rest of its run is marked
+      // empty, and the top-c reads all of dst[0, E) (no packing copy)
+      for (int i = e0 + wcnt[warp] + lane; i < e1; i += 32) dst[i] = make_int2(-1, 0);
       __syncthreads();
-      // pack the warps' runs of sums together (into src, which is free now)
-      int off = 0;
-      for (int w = 0; w < warp; ++w) off += wcnt[w];
-      const int cnt = wcnt[warp];
-      // eight loads in flight per lane (global to global)
-      for (int i0 = lane; i0 < cnt; i0 += 32 * 8) {
-        int2 tv[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) tv[u] = i0 + 32 * u < cnt ? wout[i0 + 32 * u] : make_int2(0, 0);
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-          if (i0 + 32 * u < cnt) src[off + i0 + 32 * u] = tv[u];
-      }
       if (threadIdx.x == 0) {
         int tot = 0;
         for (int w = 0; w < kSortWarps; ++w) tot += wcnt[w];
         scratch[8] = (uint32_t)tot;
       }
-      int2* t = src;
-      src = dst;
-      dst = t;
     } else {
       // each warp takes 32 consecutive elements per step; the previous id
       // comes from the neighbour lane, so a step needs one load per lane (and
@@ -976,14 +1056,16 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     const uint32_t pre[3] = {scratch[9], scratch[10], (uint32_t)U};
     __syncthreads();
     // ---- 5. top-c by estimate, rerank, top-k ----
+    // the sums: dst[0, U) compact (radix path), or dst[0, E) with empty
+    // entries (id -1) between the warps' runs (partitioned path)
     const int nc = block_topk_hist(
         [&](long i, float& v, int& id) {
           const int2 w = dst[i];
           id = w.x;
           v = __int_as_float(w.y);
-          return true;
+          return w.x >= 0;
         },
-        (long)U, a.c, cand, hist, maybe, kMaybe, scratch, pre);
+        (long)(part ? E : U), a.c, cand, hist, maybe, kMaybe, scratch, pre);
     const int ns2 = score_candidates(a, rq, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
     const int nres = block_topk_hist_sorted(
         [&](long i, float& v, int& id) {
