@@ -403,9 +403,63 @@ def profile_case(args, which):
     queries at the headline probe budget; "build-case" builds a 100k x 960
     GIST-shaped coCEOs index (n_proj 1024, n_repeats 8, top_m 100, which keeps
     the candidate pass rate of the 1M-row build) in FP32 and, with --split, in
-    split precision."""
+    split precision. The other cases run one kernel family each on a
+    SIFT-shaped index: "hash-case" CEOs-Hash (1M x 128, 2000 queries at
+    s=40), "dense-case" CEOs-Est (200k x 128, its 1.6 GB projection matrix,
+    500 queries), "stream-case" streamCEOs with exact maintenance (200k x 128
+    start, 20k inserts, 5k random deletes, one FIFO update of a second
+    stream), "bruteforce-case" the FP64 ground truth (1M x 128, 100
+    queries) and "split-case" a split-precision search (GIST-shaped 200k x
+    960, 500 queries)."""
     import ceos_gb300.CEOs as CEOs
+    from ceos_gb300 import _capi
 
+    if which == "hash-case":
+        X = sift_like(CFG["n"], CFG["d"], 7)
+        Q = sift_like(2000, CFG["d"], 8)
+        idx = CEOs.CEOs(CFG["n"], CFG["d"])
+        idx.setIndexParam(CFG["D"], CFG["R"], CFG["m"], -1, CFG["seed"])
+        idx.build_CEOs_Hash(X)
+        idx.n_probed_vectors, idx.n_cand = 40, CFG["c"]
+        idx.search_CEOs_Hash(Q, CFG["k"])
+        return {"case": which, "timings_ms": idx.last_timings()}
+    if which == "dense-case":
+        X = sift_like(200_000, CFG["d"], 7)
+        Q = sift_like(500, CFG["d"], 8)
+        idx = CEOs.CEOs(200_000, CFG["d"])
+        idx.setIndexParam(CFG["D"], CFG["R"], CFG["m"], -1, CFG["seed"])
+        idx.build(X)
+        idx.n_probed_vectors, idx.n_cand = 10, 2000
+        idx.search(Q, CFG["k"])
+        return {"case": which, "timings_ms": idx.last_timings()}
+    if which == "stream-case":
+        X = sift_like(230_000, CFG["d"], 7)
+        st = CEOs.streamCEOs(CFG["d"])
+        st.setIndexParam(CFG["D"], CFG["R"], CFG["m"], -1, CFG["seed"])
+        st.set_reserve(CFG["m"] // 2)
+        st.build(X[:200_000])
+        st.update(X[200_000:220_000])
+        st.delete(np.random.default_rng(5).choice(220_000, 5000, replace=False).astype(np.int32))
+        fifo = CEOs.streamCEOs(CFG["d"])
+        fifo.setIndexParam(CFG["D"], CFG["R"], CFG["m"], -1, CFG["seed"])
+        fifo.build(X[:200_000])
+        fifo.update(X[220_000:230_000], 10_000)
+        return {"case": which, "timings_ms": st.last_timings()}
+    if which == "bruteforce-case":
+        X = sift_like(CFG["n"], CFG["d"], 7)
+        Q = sift_like(100, CFG["d"], 8)
+        _capi.bruteforce_fp64(X, Q, CFG["k"])
+        return {"case": which}
+    if which == "split-case":
+        X = gist_like(200_000, 960, 3)
+        Q = gist_like(500, 960, 4)
+        idx = CEOs.CEOs(200_000, 960)
+        idx.setIndexParam(1024, 8, 200, -1, 42)
+        idx.precision = "split_bf16"
+        idx.build_coCEOs_Est(X)
+        idx.n_probed_vectors, idx.n_cand = 60, 4000
+        idx.search_coCEOs_Est(Q, CFG["k"])
+        return {"case": which, "timings_ms": idx.last_timings()}
     if which == "query-case":
         X = sift_like(CFG["n"], CFG["d"], 7)
         Q = sift_like(2000, CFG["d"], 8)
@@ -694,7 +748,8 @@ def main():
     ap.add_argument("--parity-queries", type=int, default=48)
     ap.add_argument("--recall-queries", type=int, default=200)
     ap.add_argument("--split", action="store_true", help="build-case in split precision")
-    ap.add_argument("--only", choices=["served", "stream", "split", "query-case", "build-case"],
+    ap.add_argument("--only", choices=["served", "stream", "split", "query-case", "build-case", "hash-case",
+                                       "dense-case", "stream-case", "bruteforce-case", "split-case"],
                     default=None,
                     help="run one secondary leg alone and print its JSON")
     ap.add_argument("--no-legs", action="store_true",
@@ -705,7 +760,7 @@ def main():
         from ceos_gb300 import _capi
 
         _capi.lib().ceos_set_log_level(0)
-        if args.only in ("query-case", "build-case"):
+        if args.only.endswith("-case"):
             leg = profile_case(args, args.only)
         else:
             leg = {"served": served_leg, "stream": stream_leg, "split": split_leg}[args.only](args)

@@ -251,8 +251,10 @@ CEOS_DEV uint32_t warp_reserve(bool want, uint32_t* counter) {
 // sorted descending without a block-wide sort. scratch[12] = 1 reports a
 // sorted result; it is 0 when a path without bin order was taken or a bin
 // holds more than kBinSortMax items (the caller sorts then).
+// kLoadsU: items each thread loads before it uses them in the passes (more
+// when the items come from HBM, at the cost of registers).
 constexpr int kBinSortMax = 24;
-template <bool kBinOrder = false, typename GetItem>
+template <bool kBinOrder = false, int kLoadsU = kTopkU, typename GetItem>
 __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32_t* hist,
                                uint64_t* maybe, int maybe_cap, uint32_t* scratch,
                                const uint32_t* pre = nullptr) {
@@ -272,19 +274,19 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   __syncthreads();
   if (!pre) {
     uint32_t lo = 0xffffffffu, hi = 0u, cnt = 0u;
-    for (long base = 0; base < N; base += kTopkU * blockDim.x) {
-      float v[kTopkU];
-      int id[kTopkU];
-      bool ok[kTopkU];
+    for (long base = 0; base < N; base += kLoadsU * blockDim.x) {
+      float v[kLoadsU];
+      int id[kLoadsU];
+      bool ok[kLoadsU];
 #pragma unroll
-      for (int u = 0; u < kTopkU; ++u) {
+      for (int u = 0; u < kLoadsU; ++u) {
         const long i = base + u * blockDim.x + threadIdx.x;
         v[u] = 0.f;
         id[u] = 0;
         ok[u] = i < N && get(i, v[u], id[u]);
       }
 #pragma unroll
-      for (int u = 0; u < kTopkU; ++u) {
+      for (int u = 0; u < kLoadsU; ++u) {
         if (ok[u]) {
           const uint32_t k = fkey(v[u]);
           lo = min(lo, k);
@@ -350,19 +352,19 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   // ---- pass 2: histogram ----
   for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) hist[b] = 0;
   __syncthreads();
-  for (long base = 0; base < N; base += kTopkU * blockDim.x) {
-    float v[kTopkU];
-    int id[kTopkU];
-    bool ok[kTopkU];
+  for (long base = 0; base < N; base += kLoadsU * blockDim.x) {
+    float v[kLoadsU];
+    int id[kLoadsU];
+    bool ok[kLoadsU];
 #pragma unroll
-    for (int u = 0; u < kTopkU; ++u) {
+    for (int u = 0; u < kLoadsU; ++u) {
       const long i = base + u * blockDim.x + threadIdx.x;
       v[u] = 0.f;
       id[u] = 0;
       ok[u] = i < N && get(i, v[u], id[u]);
     }
 #pragma unroll
-    for (int u = 0; u < kTopkU; ++u)
+    for (int u = 0; u < kLoadsU; ++u)
       if (ok[u]) atomicAdd(&hist[bin_of(v[u])], 1u);
   }
   __syncthreads();
@@ -408,19 +410,19 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   const uint32_t need = (uint32_t)K - above;
   const bool fits = inbin <= (uint32_t)maybe_cap;
   // ---- pass 3: compaction ----
-  for (long base = 0; base < N; base += kTopkU * blockDim.x) {
-    float v[kTopkU];
-    int id[kTopkU];
-    bool ok[kTopkU];
+  for (long base = 0; base < N; base += kLoadsU * blockDim.x) {
+    float v[kLoadsU];
+    int id[kLoadsU];
+    bool ok[kLoadsU];
 #pragma unroll
-    for (int u = 0; u < kTopkU; ++u) {
+    for (int u = 0; u < kLoadsU; ++u) {
       const long i = base + u * blockDim.x + threadIdx.x;
       v[u] = 0.f;
       id[u] = 0;
       ok[u] = i < N && get(i, v[u], id[u]);
     }
 #pragma unroll
-    for (int u = 0; u < kTopkU; ++u) {
+    for (int u = 0; u < kLoadsU; ++u) {
       const int b = ok[u] ? bin_of(v[u]) : -1;
       const bool sure = ok[u] && b > tb;
       const bool cand = ok[u] && b == tb && fits;

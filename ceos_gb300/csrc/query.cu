@@ -25,6 +25,8 @@
 //     accumulates the float4 chunks g, g+8, ... with FMA, then a butterfly
 //     over the 8 lanes), then the block selects the top-k, written best first
 //     with zero fill past the number of results (src/CEOs.cpp:659-666).
+#include <climits>
+
 #include "kernels.h"
 #include "common.cuh"
 
@@ -848,8 +850,21 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       __syncthreads();
       // one 32-pair step: lanes with a pair are ranked among the lanes of equal
       // digit (lanes without one get a key no digit has), in lane order
+      // Columns of a CEOs / coCEOs index hold distinct ids, and one 32-pair
+      // step reads one column, so lanes of equal digit hold different ids: their
+      // order within the partition cannot change a sum, and a shared-memory
+      // atomic places them. Stream columns (repeats) are ranked in lane order.
+      const bool atom_scatter = part && a.distinct_ids;
       auto place = [&](const int2 v, const bool has) {
         const int dg = has ? ((v.x >> shift) & (nbins - 1)) : 0;
+        if (atom_scatter) {
+          if (has) {
+            int b;
+            asm volatile("atom.shared.add.u32 %0, [%1], 1;" : "=r"(b) : "r"(smem_u32(myh + dg)) : "memory");
+            dst[b] = v;
+          }
+          return;
+        }
         const unsigned peers = __match_any_sync(0xffffffffu, has ? dg : nbins + lane);
         const int rank = __popc(peers & ((1u << lane) - 1u));
         const int b = has ? myh[dg] : 0;
@@ -915,7 +930,7 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     uint32_t klo = 0xffffffffu, khi = 0u;
     if (part) {
       // each warp: the partitions [Pa, Pb), a contiguous run [e0, e1) of src;
-      // its sums go to dst[e0 ..) first and are packed together afterwards
+      // its sums overwrite the front of the run
       const int TR = 1 << tb;
       float* tab = reinterpret_cast<float*>(sm + Lq.rhist) + (size_t)warp * kPartTable;
       uint8_t* tag = reinterpret_cast<uint8_t*>(sm + Lq.rhist + kPartTagOff) + (size_t)warp * kPartTable;
@@ -927,14 +942,11 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       const int Pa = (int)((long)warp * nbins / kSortWarps);
       const int Pb = (int)((long)(warp + 1) * nbins / kSortWarps);
       const int e0 = pstart[Pa], e1 = pstart[Pb];
-      int2* wout = dst + e0;
-      // write out the finished sum of slot `loc` (tag tg: partition Pa + tg - 1)
-      auto emit = [&](int tg, int loc, float sum) {
-        const int pos = atomicAdd(&wcnt[warp], 1);
-        wout[pos] = make_int2(((Pa + tg - 1) << tb) | loc, __float_as_int(sum));
-        klo = min(klo, fkey(sum));
-        khi = max(khi, fkey(sum));
-      };
+      // the sums are written in place over the partitioned pairs: a sum is
+      // emitted after at least one pair of its id was read, so its position
+      // (the warp's emit count) stays below every pair still to be read
+      int2* wout = src + e0;
+      int wbase = 0;
       for (int c0 = e0; c0 < e1; c0 += 32 * kU) {
         int2 v[kU];
 #pragma unroll
@@ -954,11 +966,21 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
           // (= partition, then probe) order
           const unsigned peers = __match_any_sync(0xffffffffu, act ? loc : TR + lane);
           __syncwarp();
-          if (act && __ffs(peers) - 1 == lane) {
-            int ct = tag[loc];
-            float t = tab[loc];
-            unsigned rest = peers;
-            do {
+          const bool lead = act && __ffs(peers) - 1 == lane;
+          int ct = 0;
+          float t = 0.f;
+          unsigned rest = lead ? peers : 0u;
+          if (lead) {
+            ct = tag[loc];
+            t = tab[loc];
+          }
+          // every lane takes part in each round, so the finished sums of a
+          // round get consecutive positions from one ballot
+          while (__any_sync(0xffffffffu, rest != 0u)) {
+            bool em = false;
+            int et = 0;
+            float ev = 0.f;
+            if (rest) {
               const int l = __ffs(rest) - 1;
               rest &= rest - 1u;
               const int tm = stt[l];
@@ -966,11 +988,23 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
               if (tm == ct) {
                 t = t + vm;
               } else {
-                if (ct != 0) emit(ct, loc, t);
+                em = ct != 0;  // the slot's previous id is finished
+                et = ct;
+                ev = t;
                 ct = tm;
                 t = vm;  // first value of the id as is
               }
-            } while (rest);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, em);
+            if (em) {
+              wout[wbase + __popc(m & ((1u << lane) - 1u))] =
+                  make_int2(((Pa + et - 1) << tb) | loc, __float_as_int(ev));
+              klo = min(klo, fkey(ev));
+              khi = max(khi, fkey(ev));
+            }
+            wbase += __popc(m);
+          }
+          if (lead) {
             tag[loc] = (uint8_t)ct;
             tab[loc] = t;
           }
@@ -980,12 +1014,20 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       // the slots still held
       for (int loc = lane; loc < TR; loc += 32) {
         const int ct = tag[loc];
-        if (ct != 0) emit(ct, loc, tab[loc]);
+        const unsigned m = __ballot_sync(0xffffffffu, ct != 0);
+        if (ct != 0) {
+          const float sv = tab[loc];
+          wout[wbase + __popc(m & ((1u << lane) - 1u))] = make_int2(((Pa + ct - 1) << tb) | loc, __float_as_int(sv));
+          klo = min(klo, fkey(sv));
+          khi = max(khi, fkey(sv));
+        }
+        wbase += __popc(m);
       }
+      if (lane == 0) wcnt[warp] = wbase;
       __syncwarp();
-      // the warp's sums fill dst[e0, e0 + cnt); the rest of its run is marked
-      // empty, and the top-c reads all of dst[0, E) (no packing copy)
-      for (int i = e0 + wcnt[warp] + lane; i < e1; i += 32) dst[i] = make_int2(-1, 0);
+      // the warp's sums fill src[e0, e0 + cnt); the rest of its run is marked
+      // empty, and the top-c reads all of src[0, E) (no packing copy)
+      for (int i = e0 + wcnt[warp] + lane; i < e1; i += 32) src[i] = make_int2(-1, 0);
       __syncthreads();
       if (threadIdx.x == 0) {
         int tot = 0;
@@ -1058,14 +1100,15 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     // ---- 5. top-c by estimate, rerank, top-k ----
     // the sums: dst[0, U) compact (radix path), or dst[0, E) with empty
     // entries (id -1) between the warps' runs (partitioned path)
-    const int nc = block_topk_hist(
-        [&](long i, float& v, int& id) {
-          const int2 w = dst[i];
-          id = w.x;
-          v = __int_as_float(w.y);
-          return w.x >= 0;
-        },
-        (long)(part ? E : U), a.c, cand, hist, maybe, kMaybe, scratch, pre);
+    const int2* sums = part ? src : dst;
+    auto sget = [&](long i, float& v, int& id) {
+      const int2 w = sums[i];
+      id = w.x;
+      v = __int_as_float(w.y);
+      return w.x >= 0;
+    };
+    // eight items in flight per thread: the sums come from L2 or HBM
+    const int nc = block_topk_hist<false, 8>(sget, (long)(part ? E : U), a.c, cand, hist, maybe, kMaybe, scratch, pre);
     const int ns2 = score_candidates(a, rq, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
     const int nres = block_topk_hist_sorted(
         [&](long i, float& v, int& id) {
@@ -1082,6 +1125,7 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     __syncthreads();
   }
 }
+
 
 cudaError_t launch_query_sorted(const QueryArgs& a, int grid, size_t smem, cudaStream_t st) {
   if (a.nq <= 0) return cudaSuccess;

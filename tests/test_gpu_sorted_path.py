@@ -91,6 +91,24 @@ def test_sorted_search_exact_large_ids(gpu, oracle, force_sorted, n):
     assert np.array_equal(gi, oi) and bits_equal(gd, od)
 
 
+def test_sorted_repeated_ids(gpu, oracle, force_sorted):
+    """Rows 0..149 have ten times the norm of the others, so they fill both
+    ends of every bucket: most probed pairs fall in the first partition, and
+    every one of those ids is summed over many probed buckets."""
+    n, d = 20000, 48
+    X = gist_like(n, d, seed=61)
+    X[:150] *= 10.0
+    Q = gist_like(32, d, seed=62)
+    g, o = gpu.CEOs(n, d), oracle.CEOs(n, d)
+    for idx in (g, o):
+        idx.setIndexParam(256, 4, 100, 4, 9)
+        idx.build_coCEOs_Est(X)
+        idx.n_probed_vectors, idx.n_cand = 60, 120
+    gi, gd = g.search_coCEOs_Est(Q, 10)
+    oi, od = o.search_coCEOs_Est(Q, 10)
+    assert np.array_equal(gi, oi) and bits_equal(gd, od)
+
+
 def test_sorted_matches_table_path(gpu, force_sorted):
     """Both accumulation kernels give the same bits on the same index."""
     X = sift_like(5000, 64, seed=41)
