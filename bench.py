@@ -444,7 +444,7 @@ def profile_case(args, which):
         fifo.setIndexParam(CFG["D"], CFG["R"], CFG["m"], -1, CFG["seed"])
         fifo.build(X[:200_000])
         fifo.update(X[220_000:230_000], 10_000)
-        return {"case": which, "timings_ms": st.last_timings()}
+        return {"case": which, "size": int(st.size)}
     if which == "bruteforce-case":
         X = sift_like(CFG["n"], CFG["d"], 7)
         Q = sift_like(100, CFG["d"], 8)
