@@ -40,6 +40,11 @@ cudaError_t launch_project(const ProjArgs& a, int mode, int L, int num_sms, cuda
 // Split-precision tensor-core projection (fhtDim 256 and 1024).
 bool project_tc_supported(int L);
 cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st);
+// fhtDim 1024 on tcgen05 (project_t5.cu); project_t5_take_faults returns and
+// clears the number of CTAs whose bounded waits gave up (-1 on a CUDA error),
+// synchronizing the stream.
+cudaError_t launch_project_t5(const ProjArgs& a, int mode, cudaStream_t st, int num_sms);
+int project_t5_take_faults(cudaStream_t st);
 
 // ---- selection (select.cu) ----
 // Per column of the row-major sample samp[S][C]: u32 key thresholds, the lower

@@ -1,0 +1,427 @@
+// Split-precision projection for fhtDim F = 1024 on the fifth-generation tensor
+// cores (tcgen05: operands in shared memory, accumulators in tensor memory).
+// Same outputs as k_project (ROWS / COLS / EMIT, project_impl.cuh); no
+// reference counterpart (the reference's FFHT is CPU code, src/fht.c).
+//
+// With Sylvester ordering H_1024 = H_128 (x) H_8: a vector x read as the
+// 128 x 8 row-major matrix X transforms as H_128 . X . H_8. Each of the three
+// rounds of a repeat, y = H_1024 (s (.) x), is
+//   W = (S (.) X) . H_8          CUDA cores: sign flip, three butterfly stages
+//   Y = H_128 . W                one tcgen05.mma product, K = 256
+// for a tile of 16 vectors at once: the B operand holds W of all 16 vectors
+// (N = 16 x 8 = 128 columns n = 8 v + j, MN-major in shared memory), A is
+// [H_128 | H_128] (M = 128, K-major, written once), and W enters split into
+// bfloat16 hi = bf16(w) (K rows 0..127) and lo = bf16(w - hi) (K rows
+// 128..255), so the FP32 accumulator receives H . hi + H . lo. The +-1 entries
+// of H are exact in bfloat16.
+//
+// Thread t = 32 q + l of warp w = 4 c + q (c = t / 128) owns row i = 32 q + l of
+// every vector in columns 32 c .. 32 c + 31 of the accumulator, i.e. vectors
+// 4 c .. 4 c + 3: tensor-memory lane i is the row that H_128 produced, and
+// its 8 values per vector are exactly the row that H_8 mixes next, so no
+// transposes are needed between rounds, and each thread writes its hi and lo
+// values of a vector as one 16-byte store.
+//
+// Two tiles are in flight per CTA (one CTA of 512 threads per SM): the threads
+// prepare one tile's operand while the tensor core multiplies the other's.
+// Tensor memory holds the two 128-column accumulators and, in the other 256
+// columns, the two tiles' input rows, staged once per tile and read back at
+// the start of every repeat (each thread its own lane and 32 columns). Each
+// thread waits for a product on its mbarrier itself, so a step has a single
+// CTA barrier, before the next product is issued. Every wait is bounded; a
+// wait that gives up records a fault (read by project_t5_take_faults), waits a
+// bounded time for the CTA's products in flight, frees the tensor memory and
+// ends the CTA.
+#include "kernels.h"
+#include "common.cuh"
+#include "emit.cuh"
+
+namespace ceos {
+
+namespace {
+
+constexpr int kT5Threads = 512;
+constexpr int kT5Vec = 16;         // vectors per tile
+constexpr int kT5N = kT5Vec * 8;   // accumulator columns per tile
+constexpr int kT5K = 256;          // hi and lo rows of the 128-row operand
+// A = [H | H]: M = 128 x K = 256 bfloat16, K-major core matrices (8 rows of 16
+// bytes along K), 8-K groups 128 bytes apart, 8-row groups 4096 bytes apart
+constexpr uint32_t kALbo = 128;
+constexpr uint32_t kASbo = 4096;
+constexpr uint32_t kABytes = 128 * kT5K * 2;
+// B = W: N = 128 x K = 256 bfloat16, MN-major core matrices (8 columns of 16
+// bytes along N), 8-column groups 128 bytes apart, 8-K groups 2048 bytes apart
+constexpr uint32_t kBGroupN = 128;
+constexpr uint32_t kBGroupK = 2048;
+constexpr uint32_t kBBytes = kT5N * kT5K * 2;
+constexpr uint32_t kOffA = 0;
+constexpr uint32_t kOffB = kOffA + kABytes;        // two operand buffers
+constexpr uint32_t kOffBar = kOffB + 2 * kBBytes;  // two mbarriers + tmem holder
+constexpr uint32_t kSmem = kOffBar + 64;
+constexpr int kTmemCols = 4 * kT5N;  // accumulators, then staged inputs
+// Instruction descriptor (kind::f16): D FP32 (bits 4-5 = 1), A and B
+// bfloat16 (bits 7-9, 10-12 = 1), A K-major (bit 15 = 0), B MN-major (bit 16),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((uint32_t)(kT5N >> 3) << 17) |
+                            ((128u >> 4) << 24);
+// a wait gives up after this many polls of at most kWaitHintNs each (far
+// beyond any product's latency)
+constexpr int kWaitPolls = 1 << 16;
+constexpr uint32_t kWaitHintNs = 20000;
+
+__device__ unsigned g_t5_faults = 0;
+
+CEOS_DEV uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor: start address, leading-dimension byte
+// offset (between core-matrix groups along K) and stride-dimension byte
+// offset (between groups along M / N), no swizzle, descriptor version 1.
+CEOS_DEV uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+CEOS_DEV bool bar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < kWaitPolls; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(kWaitHintNs)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+CEOS_DEV void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+CEOS_DEV void tmem_st32(uint32_t taddr, const float (&v)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]),
+      "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]),
+      "f"(v[17]), "f"(v[18]), "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]),
+      "f"(v[25]), "f"(v[26]), "f"(v[27]), "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// (lo, hi) -> bfloat16x2 with lo in the low half, rounded to nearest even
+CEOS_DEV uint32_t bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+}  // namespace
+
+template <int MODE>
+__global__ void __launch_bounds__(kT5Threads, 1) k_project_t5(ProjArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int t = threadIdx.x, w = t >> 5, l = t & 31;
+  const int q = w & 3;          // lane quarter of the tensor memory
+  const int cg = w >> 2;        // column group: vectors 4 cg .. 4 cg + 3 of a tile
+  const int row = 32 * q + l;   // the row i of X (and lane of the accumulator)
+  unsigned char* sA = sm + kOffA;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kOffBar);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(sm + kOffBar + 16);
+  const int R = a.R, D = a.D, C = a.R * a.D;
+
+  // A = [H | H]: element (m, k) = (-1)^popc(m & (k mod 128))
+  for (int e = t; e < 128 * kT5K / 8; e += kT5Threads) {
+    const int m = e / (kT5K / 8), kg = e % (kT5K / 8);  // row, 8-K group
+    uint32_t wv[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      uint32_t h2 = 0;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = (kg * 8 + 2 * p + h) & 127;
+        const uint32_t hv = (__popc(m & k) & 1) ? 0xBF80u : 0x3F80u;
+        h2 |= hv << (16 * h);
+      }
+      wv[p] = h2;
+    }
+    *reinterpret_cast<uint4*>(sA + (m & 7) * 16 + (m >> 3) * kASbo + kg * kALbo) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar + 1)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(holder)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *holder;
+  // this thread's lane quarter and its 32 columns of slot s's accumulator, and
+  // of slot s's staged input rows
+  auto my_tmem = [&](int s) { return tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(s * kT5N + 32 * cg); };
+  auto my_input = [&](int s) { return my_tmem(s) + (uint32_t)(2 * kT5N); };
+
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  bool fault = false;
+  const long n_tiles = (a.n_rows + kT5Vec - 1) / kT5Vec;
+  const int steps = 3 * R;
+
+  // row pointer of vector v (0..15) of tile `tile`, null past n_rows
+  auto vec_src = [&](long tile, int v, long& rid) -> const float* {
+    const long r = tile * kT5Vec + v;
+    rid = r;
+    if (tile < 0 || r >= a.n_rows) return nullptr;
+    long src = a.row_map ? a.row_map[r] : r;
+    src += a.head;
+    if (src >= a.cap_rows) src -= a.cap_rows;
+    return a.X + src * a.ldx;
+  };
+
+  // outputs of repeat rr held in x (this thread's row, 4 vectors x 8)
+  auto output = [&](long tile, int rr, const float (&x)[32]) {
+    const int idx0 = row * 8;  // output index of j = 0
+#pragma unroll
+    for (int vv = 0; vv < 4; ++vv) {
+      long rid;
+      const float* src = vec_src(tile, 4 * cg + vv, rid);
+      if (src == nullptr) continue;
+      if constexpr (MODE == PROJ_EMIT) {
+        const long id = a.id_base + (a.row_map ? a.row_map[rid] : rid);
+        uint32_t hit = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int idx = idx0 + j;
+          if (idx < D && emit_maybe(x[8 * vv + j], __ldg(a.thf + rr * D + idx))) hit |= 1u << j;
+        }
+#pragma unroll 1
+        while (hit) {
+          const int j = __ffs(hit) - 1;
+          hit &= hit - 1u;
+          float xv = x[8 * vv];
+#pragma unroll
+          for (int jj = 1; jj < 8; ++jj)
+            if (jj == j) xv = x[8 * vv + jj];
+          emit_exact(a, rr * D + idx0 + j, xv, (int)id);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int idx = idx0 + j;
+          if (idx >= D) continue;
+          const int col = rr * D + idx;
+          if constexpr (MODE == PROJ_ROWS) {
+            a.out[rid * (long)C + col] = x[8 * vv + j];
+          } else {  // PROJ_COLS
+            const int slot = a.col_slot ? a.col_slot[col] : col;
+            if (slot >= 0) a.out[(long)slot * a.ld_out + rid] = x[8 * vv + j];
+          }
+        }
+      }
+    }
+  };
+
+  // this thread's input values of slot s's tile (4 vectors x 8, zero past
+  // ldx and n_rows), staged in tensor memory for the tile's repeats
+  auto stage = [&](int s, long tile) {
+    float x[32];
+    // (ldx is a multiple of 8, so a row's 8 values are all inside or all past it)
+#pragma unroll
+    for (int vv = 0; vv < 4; ++vv) {
+      long rid;
+      const float* src = vec_src(tile, 4 * cg + vv, rid);
+      float4 u0 = make_float4(0.f, 0.f, 0.f, 0.f), u1 = u0;
+      if (src != nullptr && row * 8 < a.ldx) {
+        u0 = __ldg(reinterpret_cast<const float4*>(src + row * 8));
+        u1 = __ldg(reinterpret_cast<const float4*>(src + row * 8 + 4));
+      }
+      x[8 * vv + 0] = u0.x;
+      x[8 * vv + 1] = u0.y;
+      x[8 * vv + 2] = u0.z;
+      x[8 * vv + 3] = u0.w;
+      x[8 * vv + 4] = u1.x;
+      x[8 * vv + 5] = u1.y;
+      x[8 * vv + 6] = u1.z;
+      x[8 * vv + 7] = u1.w;
+    }
+    tmem_st32(my_input(s), x);
+  };
+
+  // One step of slot s (tile `tile`): the previous product's result (or the
+  // staged input), sign flip of round `rnd` of repeat `rr`, H_8, split,
+  // operand store; then the product. Returns false (for every thread) when a
+  // wait gave up.
+  auto step = [&](int s, long tile, int st) -> bool {
+    float x[32];
+    const int rr = st / 3, rnd = st % 3;
+    bool ok = true;
+    if (st > 0) {
+      ok = bar_wait(su32(bar + s), phase[s]);
+      if (ok) phase[s] ^= 1u;  // a product still pending keeps its parity
+      pending[s] = !ok;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      tmem_ld32(my_tmem(s), x);
+      if (rnd == 0 && ok) output(tile, rr - 1, x);
+    }
+    if (rnd == 0) tmem_ld32(my_input(s), x);
+    // signs of elements 8 i .. 8 i + 7 (bit set: +1)
+    const uint32_t sw = __ldg(a.signs + (size_t)(rr * 3 + rnd) * 32 + (row >> 2)) >> ((row & 3) * 8);
+#pragma unroll
+    for (int vv = 0; vv < 4; ++vv) {
+      float y[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        y[j] = __uint_as_float(__float_as_uint(x[8 * vv + j]) ^ ((~sw << (31 - j)) & 0x80000000u));
+      // H_8 along the row (natural order)
+#pragma unroll
+      for (int h = 1; h < 8; h <<= 1) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (j & h) continue;
+          const float u = y[j], v = y[j + h];
+          y[j] = u + v;
+          y[j + h] = u - v;
+        }
+      }
+      uint32_t hi[4], lo[4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        hi[p] = bf16x2(y[2 * p], y[2 * p + 1]);
+        const float h0 = __uint_as_float(hi[p] << 16), h1 = __uint_as_float(hi[p] & 0xffff0000u);
+        lo[p] = bf16x2(y[2 * p] - h0, y[2 * p + 1] - h1);
+      }
+      // column n = 8 (4 cg + vv) + j of K rows i (hi) and 128 + i (lo)
+      unsigned char* pb = sm + kOffB + (uint32_t)s * kBBytes + (uint32_t)(4 * cg + vv) * kBGroupN +
+                          (uint32_t)(row & 7) * 16 + (uint32_t)(row >> 3) * kBGroupK;
+      *reinterpret_cast<uint4*>(pb) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(pb + 16 * kBGroupK) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    if (__syncthreads_or(!ok)) return false;
+    if (t == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d = tmem + (uint32_t)(s * kT5N);
+      const uint32_t b0 = su32(sm + kOffB + (uint32_t)s * kBBytes);
+#pragma unroll
+      for (int kk = 0; kk < kT5K / 16; ++kk) {
+        const uint64_t da = smem_desc(su32(sA) + kk * 2 * kALbo, kALbo, kASbo);
+        const uint64_t db = smem_desc(b0 + kk * 2 * kBGroupK, kBGroupK, kBGroupN);
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+            "l"(da), "l"(db), "r"(kIdesc), "r"(kk)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       su32(bar + s))
+                   : "memory");
+    }
+    pending[s] = true;
+    return true;
+  };
+
+  // the last repeat's outputs of slot s
+  auto finish = [&](int s, long tile) -> bool {
+    float x[32];
+    const bool ok = bar_wait(su32(bar + s), phase[s]);
+    if (ok) phase[s] ^= 1u;
+    pending[s] = !ok;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem_ld32(my_tmem(s), x);
+    if (ok) output(tile, R - 1, x);
+    return !__syncthreads_or(!ok);
+  };
+
+  for (long t0 = 2L * blockIdx.x; t0 < n_tiles && !fault; t0 += 2L * gridDim.x) {
+    const long tl[2] = {t0, t0 + 1 < n_tiles ? t0 + 1 : -1};
+    stage(0, tl[0]);
+    stage(1, tl[1]);
+    for (int st = 0; st < steps && !fault; ++st) {
+      for (int s = 0; s < 2; ++s) {
+        if (!step(s, tl[s], st)) {  // uniform across the CTA
+          fault = true;
+          break;
+        }
+      }
+    }
+    if (!fault) {
+      for (int s = 0; s < 2; ++s) {
+        if (!finish(s, tl[s])) {
+          fault = true;
+          break;
+        }
+      }
+    }
+    // the accumulators are read before the next pair overwrites them
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (fault) {
+    // let products still in flight finish (bounded) before the tensor memory
+    // is released
+    for (int s = 0; s < 2; ++s)
+      if (pending[s]) bar_wait(su32(bar + s), phase[s]);
+    if (t == 0) atomicAdd(&g_t5_faults, 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (w == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+template <int MODE>
+static cudaError_t launch_t5(const ProjArgs& a, int num_sms, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_project_t5<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  if (e != cudaSuccess) return e;
+  const long pairs = (a.n_rows + 2 * kT5Vec - 1) / (2 * kT5Vec);
+  long blocks = num_sms;  // one CTA per SM (shared memory and tensor memory)
+  if (blocks > pairs) blocks = pairs;
+  if (blocks < 1) blocks = 1;
+  k_project_t5<MODE><<<(unsigned)blocks, kT5Threads, kSmem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_t5(const ProjArgs& a, int mode, cudaStream_t st, int num_sms) {
+  if (a.n_rows <= 0) return cudaSuccess;
+  switch (mode) {
+    case PROJ_ROWS: return launch_t5<PROJ_ROWS>(a, num_sms, st);
+    case PROJ_COLS: return launch_t5<PROJ_COLS>(a, num_sms, st);
+    case PROJ_EMIT: return launch_t5<PROJ_EMIT>(a, num_sms, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+int project_t5_take_faults(cudaStream_t st) {
+  unsigned h = 0, zero = 0;
+  if (cudaMemcpyFromSymbolAsync(&h, g_t5_faults, sizeof(h), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  if (h) cudaMemcpyToSymbolAsync(g_t5_faults, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, st);
+  return (int)h;
+}
+
+}  // namespace ceos

@@ -25,6 +25,8 @@
 // and writes its accumulator to tensor memory, so every product would be a
 // TMEM -> register -> shared memory round trip plus an mbarrier wait; the
 // register-resident chain here has no such traffic.
+#include <cstdlib>
+
 #include "kernels.h"
 #include "common.cuh"
 #include "emit.cuh"
@@ -291,6 +293,11 @@ bool project_tc_supported(int L) { return L == 8 || L == 10; }
 cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st) {
   if (a.n_rows <= 0) return cudaSuccess;
   if (L == 10) {
+    static const bool t5 = [] {
+      const char* e = std::getenv("CEOS_GB300_T5");
+      return e && e[0] == '1';
+    }();
+    if (t5) return launch_project_t5(a, mode, st, num_sms);
     switch (mode) {
       case PROJ_ROWS: return launch_tc<32, PROJ_ROWS>(a, num_sms, st);
       case PROJ_COLS: return launch_tc<32, PROJ_COLS>(a, num_sms, st);

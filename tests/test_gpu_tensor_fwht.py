@@ -68,13 +68,16 @@ def test_tensor_build_recall_matches_fp32(gpu, oracle):
     assert same > 0.98, same
 
 
-def test_tensor_sampled_build_selects_exactly(gpu):
+@pytest.mark.parametrize("d,D,R", [(150, 128, 2),    # fhtDim 256
+                                   (300, 1024, 1)])  # fhtDim 1024
+def test_tensor_sampled_build_selects_exactly(gpu, d, D, R):
     """n > 65536 takes the sampled-threshold build; with the tensor-core
     projection its buckets must be exactly the two-ended top-m of the
     split-precision projections themselves. The dense build of the same index
-    produces the same projection values, and the order is the library's: key
-    of the value, then the smaller id."""
-    n, d, D, R, m = 70000, 150, 128, 2, 64
+    produces the same projection values (column dump, row sample and fused
+    emission all run the same kernel), and the order is the library's: key of
+    the value, then the smaller id."""
+    n, m = 70000, 64
     X = netflix_like(n, d, seed=17)
     dense = gpu.CEOs(n, d)
     dense.setIndexParam(D, R, m, 1, 23)
