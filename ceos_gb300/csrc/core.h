@@ -388,6 +388,12 @@ struct Core {
     e.cap = (int)cap;
     CUDA_TRY(launch_project(e, PROJ_EMIT, L, sms, stream));
     timer.mark("project+emit");
+    if (e.tensor && L == 10) {
+      // the tensor-core projection ends a CTA whose bounded wait gave up
+      const int faults = project_t5_take_faults(stream);
+      if (faults != 0)
+        return fail(CEOS_ERR_CUDA, "tensor-core projection: %d blocks stopped at a wait that did not complete", faults);
+    }
     CUDA_TRY(dBids.ensure((size_t)Cc * 2 * m * 4));
     CUDA_TRY(dBvals.ensure((size_t)Cc * 2 * m * 4));
     CUDA_TRY(launch_finish_buckets(cand.as<uint64_t>(), cnt.as<unsigned>(), (int)cap, Cc, m,

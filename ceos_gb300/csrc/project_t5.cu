@@ -15,23 +15,25 @@
 // 128..255), so the FP32 accumulator receives H . hi + H . lo. The +-1 entries
 // of H are exact in bfloat16.
 //
-// Thread t = 32 q + l of warp w = 4 c + q (c = t / 128) owns row i = 32 q + l of
-// every vector in columns 32 c .. 32 c + 31 of the accumulator, i.e. vectors
-// 4 c .. 4 c + 3: tensor-memory lane i is the row that H_128 produced, and
-// its 8 values per vector are exactly the row that H_8 mixes next, so no
-// transposes are needed between rounds, and each thread writes its hi and lo
-// values of a vector as one 16-byte store.
+// One CTA per SM: 16 compute warps and one warp that issues the products.
+// Two tiles are in flight: compute warps 8 g .. 8 g + 7 serve slot g. Warp w
+// owns tensor-memory lane quarter q = w mod 4, i.e. row i = 32 q + l of the
+// tile's vectors, for column half c = (w / 4) mod 2 (vectors 8 c .. 8 c + 7):
+// lane i of the accumulator is the row that H_128 produced, and its 8 values
+// per vector are exactly the row that H_8 mixes next, so no transposes are
+// needed between rounds, and each thread writes its hi and lo values of a
+// vector as one 16-byte store. While one group prepares its slot's operand,
+// the tensor core multiplies the other's.
 //
-// Two tiles are in flight per CTA (one CTA of 512 threads per SM): the threads
-// prepare one tile's operand while the tensor core multiplies the other's.
 // Tensor memory holds the two 128-column accumulators and, in the other 256
 // columns, the two tiles' input rows, staged once per tile and read back at
-// the start of every repeat (each thread its own lane and 32 columns). Each
-// thread waits for a product on its mbarrier itself, so a step has a single
-// CTA barrier, before the next product is issued. Every wait is bounded; a
-// wait that gives up records a fault (read by project_t5_take_faults), waits a
-// bounded time for the CTA's products in flight, frees the tensor memory and
-// ends the CTA.
+// the start of every repeat (each thread its own lane and columns). The
+// groups and the issuing warp synchronize through mbarriers only: full[g]
+// (one arrival per compute warp of group g, after its operand stores are
+// fenced for the tensor core) and done[g] (tcgen05.commit of the product).
+// Every wait is bounded and also gives up once the other side has recorded a
+// fault; the fault (read by project_t5_take_faults) ends the CTA after a
+// bounded wait for its products in flight, and the tensor memory is freed.
 #include "kernels.h"
 #include "common.cuh"
 #include "emit.cuh"
@@ -40,7 +42,7 @@ namespace ceos {
 
 namespace {
 
-constexpr int kT5Threads = 512;
+constexpr int kT5Threads = 512;  // compute threads; one more warp issues the products
 constexpr int kT5Vec = 16;         // vectors per tile
 constexpr int kT5N = kT5Vec * 8;   // accumulator columns per tile
 constexpr int kT5K = 256;          // hi and lo rows of the 128-row operand
@@ -56,7 +58,7 @@ constexpr uint32_t kBGroupK = 2048;
 constexpr uint32_t kBBytes = kT5N * kT5K * 2;
 constexpr uint32_t kOffA = 0;
 constexpr uint32_t kOffB = kOffA + kABytes;        // two operand buffers
-constexpr uint32_t kOffBar = kOffB + 2 * kBBytes;  // two mbarriers + tmem holder
+constexpr uint32_t kOffBar = kOffB + 2 * kBBytes;  // four mbarriers, tmem holder, fault flag
 constexpr uint32_t kSmem = kOffBar + 64;
 constexpr int kTmemCols = 4 * kT5N;  // accumulators, then staged inputs
 // Instruction descriptor (kind::f16): D FP32 (bits 4-5 = 1), A and B
@@ -64,10 +66,10 @@ constexpr int kTmemCols = 4 * kT5N;  // accumulators, then staged inputs
 // N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((uint32_t)(kT5N >> 3) << 17) |
                             ((128u >> 4) << 24);
-// a wait gives up after this many polls of at most kWaitHintNs each (far
-// beyond any product's latency)
-constexpr int kWaitPolls = 1 << 16;
-constexpr uint32_t kWaitHintNs = 20000;
+// a wait gives up after this many polls (each returns within a short,
+// system-dependent time; together far beyond any product's latency)
+constexpr int kWaitPolls = 1 << 24;
+constexpr uint32_t kWaitHintNs = 20000;  // the fault path's waits: suspend hint
 
 __device__ unsigned g_t5_faults = 0;
 
@@ -79,20 +81,6 @@ CEOS_DEV uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_share
 CEOS_DEV uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
-}
-
-CEOS_DEV bool bar_wait(uint32_t bar, uint32_t parity) {
-  for (int it = 0; it < kWaitPolls; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity), "r"(kWaitHintNs)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
 }
 
 CEOS_DEV void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -133,19 +121,27 @@ CEOS_DEV uint32_t bf16x2(float lo, float hi) {
 }  // namespace
 
 template <int MODE>
-__global__ void __launch_bounds__(kT5Threads, 1) k_project_t5(ProjArgs a) {
+__global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const int t = threadIdx.x, w = t >> 5, l = t & 31;
-  const int q = w & 3;          // lane quarter of the tensor memory
-  const int cg = w >> 2;        // column group: vectors 4 cg .. 4 cg + 3 of a tile
+  const bool mma_warp = w == kT5Threads / 32;  // the last warp issues the products
+  // compute warp w serves slot g = w / 8; within its group it owns lane
+  // quarter q of the tensor memory and column half ch (vectors 8 ch .. 8 ch + 7)
+  const int g = (w >> 3) & 1;
+  const int q = w & 3;
+  const int ch = (w >> 2) & 1;
   const int row = 32 * q + l;   // the row i of X (and lane of the accumulator)
   unsigned char* sA = sm + kOffA;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kOffBar);
-  uint32_t* holder = reinterpret_cast<uint32_t*>(sm + kOffBar + 16);
+  // full[s]: slot s's operand is written (one arrival per compute warp);
+  // done[s]: slot s's product has completed (tcgen05.commit)
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + kOffBar);
+  uint64_t* done = full + 2;
+  uint32_t* holder = reinterpret_cast<uint32_t*>(sm + kOffBar + 32);
+  volatile int* fault_flag = reinterpret_cast<volatile int*>(sm + kOffBar + 36);
   const int R = a.R, D = a.D, C = a.R * a.D;
 
   // A = [H | H]: element (m, k) = (-1)^popc(m & (k mod 128))
-  for (int e = t; e < 128 * kT5K / 8; e += kT5Threads) {
+  for (int e = t; e < 128 * kT5K / 8; e += blockDim.x) {
     const int m = e / (kT5K / 8), kg = e % (kT5K / 8);  // row, 8-K group
     uint32_t wv[4];
 #pragma unroll
@@ -162,11 +158,14 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_project_t5(ProjArgs a) {
     *reinterpret_cast<uint4*>(sA + (m & 7) * 16 + (m >> 3) * kASbo + kg * kALbo) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
   }
   if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar)) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(bar + 1)) : "memory");
+    for (int s = 0; s < 2; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(full + s)), "r"(kT5Threads / 64) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(done + s)) : "memory");
+    }
+    *fault_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (w == 0) {
+  if (mma_warp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(holder)),
                  "r"(kTmemCols)
                  : "memory");
@@ -177,218 +176,302 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_project_t5(ProjArgs a) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *holder;
-  // this thread's lane quarter and its 32 columns of slot s's accumulator, and
-  // of slot s's staged input rows
-  auto my_tmem = [&](int s) { return tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(s * kT5N + 32 * cg); };
-  auto my_input = [&](int s) { return my_tmem(s) + (uint32_t)(2 * kT5N); };
-
-  uint32_t phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
-  bool fault = false;
   const long n_tiles = (a.n_rows + kT5Vec - 1) / kT5Vec;
   const int steps = 3 * R;
 
-  // row pointer of vector v (0..15) of tile `tile`, null past n_rows
-  auto vec_src = [&](long tile, int v, long& rid) -> const float* {
-    const long r = tile * kT5Vec + v;
-    rid = r;
-    if (tile < 0 || r >= a.n_rows) return nullptr;
-    long src = a.row_map ? a.row_map[r] : r;
-    src += a.head;
-    if (src >= a.cap_rows) src -= a.cap_rows;
-    return a.X + src * a.ldx;
+  // a bounded wait that also gives up once the other side has faulted (no
+  // suspend hint: a product takes about a microsecond, and a suspended warp
+  // wakes later than a polling one)
+  auto wait = [&](uint64_t* b, uint32_t parity) -> bool {
+    for (int it = 0; it < kWaitPolls; ++it) {
+      uint32_t ok;
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}\n"
+          : "=r"(ok)
+          : "r"(su32(b)), "r"(parity)
+          : "memory");
+      if (ok) return true;
+      if (*fault_flag) return false;
+    }
+    *fault_flag = 1;
+    return false;
   };
 
-  // outputs of repeat rr held in x (this thread's row, 4 vectors x 8)
-  auto output = [&](long tile, int rr, const float (&x)[32]) {
-    const int idx0 = row * 8;  // output index of j = 0
+  if (mma_warp) {
+    // ---- the product issuer: one elected lane ----
+    uint32_t fph[2] = {0u, 0u};
+    int issued[2] = {0, 0};  // commits per slot
+    bool ok = true;
+    for (long t0 = 2L * blockIdx.x; t0 < n_tiles && ok; t0 += 2L * gridDim.x) {
+      for (int st = 0; st < steps && ok; ++st) {
+        for (int s = 0; s < 2 && ok; ++s) {
+          ok = wait(full + s, fph[s]);
+          ok = __all_sync(0xffffffffu, ok);
+          if (!ok) break;
+          fph[s] ^= 1u;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          if (l == 0) {
+            const uint32_t d = tmem + (uint32_t)(s * kT5N);
+            const uint32_t b0 = su32(sm + kOffB + (uint32_t)s * kBBytes);
 #pragma unroll
-    for (int vv = 0; vv < 4; ++vv) {
-      long rid;
-      const float* src = vec_src(tile, 4 * cg + vv, rid);
-      if (src == nullptr) continue;
+            for (int kk = 0; kk < kT5K / 16; ++kk) {
+              const uint64_t da = smem_desc(su32(sA) + kk * 2 * kALbo, kALbo, kASbo);
+              const uint64_t db = smem_desc(b0 + kk * 2 * kBGroupK, kBGroupK, kBGroupN);
+              asm volatile(
+                  "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+                  "l"(da), "l"(db), "r"(kIdesc), "r"(kk)
+                  : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             su32(done + s))
+                         : "memory");
+          }
+          __syncwarp();
+          ++issued[s];
+        }
+      }
+    }
+    if (!ok) {
+      // products still in flight finish (bounded) before the tensor memory
+      // is released: wait for every commit of each slot
+      for (int s = 0; s < 2; ++s) {
+        if (issued[s] == 0) continue;
+        const uint32_t last = (uint32_t)((issued[s] - 1) & 1);
+        for (int it = 0; it < (1 << 16); ++it) {
+          uint32_t r;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+              "selp.u32 %0, 1, 0, p;\n\t}\n"
+              : "=r"(r)
+              : "r"(su32(done + s)), "r"(last), "r"(kWaitHintNs)
+              : "memory");
+          if (r) break;
+        }
+      }
+    }
+  } else {
+    // ---- the compute warps: group g prepares slot g's operands ----
+    // this thread's lane quarter and its 32 columns of chunk c (vectors
+    // 8 ch + 4 c .. + 3) of the accumulator, and of the staged input rows
+    auto my_tmem = [&](int c) { return tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * kT5N + 64 * ch + 32 * c); };
+    auto my_input = [&](int c) { return my_tmem(c) + (uint32_t)(2 * kT5N); };
+    uint32_t dph = 0u;
+
+    // row pointer of vector v (0..15) of tile `tile`, null past n_rows
+    auto vec_src = [&](long tile, int v, long& rid) -> const float* {
+      const long r = tile * kT5Vec + v;
+      rid = r;
+      if (tile < 0 || r >= a.n_rows) return nullptr;
+      long src = a.row_map ? a.row_map[r] : r;
+      src += a.head;
+      if (src >= a.cap_rows) src -= a.cap_rows;
+      return a.X + src * a.ldx;
+    };
+
+    // outputs of repeat rr held in x (this thread's row of vectors v0 .. v0 + 3);
+    // thb: the float bounds of the 8 output columns (PROJ_EMIT)
+    auto output = [&](long tile, int v0, int rr, const float (&x)[32], const float2 (&thb)[8]) {
+      const int idx0 = row * 8;  // output index of j = 0
       if constexpr (MODE == PROJ_EMIT) {
-        const long id = a.id_base + (a.row_map ? a.row_map[rid] : rid);
+        // bit 8 vv + j: value j of vector v0 + vv passes the float prefilter
         uint32_t hit = 0;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int idx = idx0 + j;
-          if (idx < D && emit_maybe(x[8 * vv + j], __ldg(a.thf + rr * D + idx))) hit |= 1u << j;
-        }
+        for (int e = 0; e < 32; ++e)
+          if (idx0 + (e & 7) < D && emit_maybe(x[e], thb[e & 7])) hit |= 1u << e;
+        // the few flagged values, one at a time (the loop stays rolled: every
+        // warp of the SM shares the instruction cache)
 #pragma unroll 1
         while (hit) {
-          const int j = __ffs(hit) - 1;
+          const int e = __ffs(hit) - 1;
           hit &= hit - 1u;
-          float xv = x[8 * vv];
+          const int j = e & 7;
+          long rid;
+          if (vec_src(tile, v0 + (e >> 3), rid) == nullptr) continue;
+          const int col = rr * D + idx0 + j;
+          if (a.col_active && !a.col_active[col]) continue;
+          float v = x[0];
 #pragma unroll
-          for (int jj = 1; jj < 8; ++jj)
-            if (jj == j) xv = x[8 * vv + jj];
-          emit_exact(a, rr * D + idx0 + j, xv, (int)id);
+          for (int i = 1; i < 32; ++i)
+            if (i == e) v = x[i];
+          float2 bj = thb[0];
+#pragma unroll
+          for (int i = 1; i < 8; ++i)
+            if (i == j) bj = thb[i];
+          const int id = (int)(a.id_base + (a.row_map ? a.row_map[rid] : rid));
+          // For a finite nonzero v the float bounds are exact (thb holds the
+          // floats of the threshold keys, emit_bounds); zeros (-0 ranks below
+          // +0) and infinities take the key test.
+          bool close, far;
+          if (v != 0.0f && isfinite(v)) {
+            close = v >= bj.x;
+            far = v <= bj.y;
+          } else {
+            const uint2 th = __ldg(reinterpret_cast<const uint2*>(a.th) + col);
+            close = fkey(v) >= th.x;
+            far = fkey(-v) >= th.y;
+          }
+          const unsigned pc = close ? atomicAdd(&a.cnt[2 * col], 1u) : 0xffffffffu;
+          const unsigned pf = far ? atomicAdd(&a.cnt[2 * col + 1], 1u) : 0xffffffffu;
+          if (pc < (unsigned)a.cap) a.cand[(2L * col) * a.cap + pc] = pack_key(v, id);
+          if (pf < (unsigned)a.cap) a.cand[(2L * col + 1) * a.cap + pf] = pack_key(-v, id);
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int idx = idx0 + j;
-          if (idx >= D) continue;
-          const int col = rr * D + idx;
-          if constexpr (MODE == PROJ_ROWS) {
-            a.out[rid * (long)C + col] = x[8 * vv + j];
-          } else {  // PROJ_COLS
-            const int slot = a.col_slot ? a.col_slot[col] : col;
-            if (slot >= 0) a.out[(long)slot * a.ld_out + rid] = x[8 * vv + j];
+        for (int vv = 0; vv < 4; ++vv) {
+          long rid;
+          if (vec_src(tile, v0 + vv, rid) == nullptr) continue;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int idx = idx0 + j;
+            if (idx >= D) continue;
+            const int col = rr * D + idx;
+            if constexpr (MODE == PROJ_ROWS) {
+              a.out[rid * (long)C + col] = x[8 * vv + j];
+            } else {  // PROJ_COLS
+              const int slot = a.col_slot ? a.col_slot[col] : col;
+              if (slot >= 0) a.out[(long)slot * a.ld_out + rid] = x[8 * vv + j];
+            }
+          }
+        }
+      }
+    };
+    // the float bounds of repeat rr's 8 output columns of this thread's row
+    auto bounds = [&](int rr, float2 (&thb)[8]) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int idx = row * 8 + j;
+        thb[j] = (MODE == PROJ_EMIT && idx < D) ? __ldg(a.thf + rr * D + idx) : make_float2(0.f, 0.f);
+      }
+    };
+
+    // this thread's input values of the group's tile (2 chunks x 4 vectors x
+    // 8, zero past ldx and n_rows), staged in tensor memory for its repeats
+    auto stage = [&](long tile) {
+#pragma unroll 1
+      for (int c = 0; c < 2; ++c) {
+        float x[32];
+        // (ldx is a multiple of 8, so a row's 8 values are all inside or all past it)
+#pragma unroll
+        for (int vv = 0; vv < 4; ++vv) {
+          long rid;
+          const float* src = vec_src(tile, 8 * ch + 4 * c + vv, rid);
+          float4 u0 = make_float4(0.f, 0.f, 0.f, 0.f), u1 = u0;
+          if (src != nullptr && row * 8 < a.ldx) {
+            u0 = __ldg(reinterpret_cast<const float4*>(src + row * 8));
+            u1 = __ldg(reinterpret_cast<const float4*>(src + row * 8 + 4));
+          }
+          x[8 * vv + 0] = u0.x;
+          x[8 * vv + 1] = u0.y;
+          x[8 * vv + 2] = u0.z;
+          x[8 * vv + 3] = u0.w;
+          x[8 * vv + 4] = u1.x;
+          x[8 * vv + 5] = u1.y;
+          x[8 * vv + 6] = u1.z;
+          x[8 * vv + 7] = u1.w;
+        }
+        tmem_st32(my_input(c), x);
+      }
+    };
+
+    // slot g's last product has completed
+    auto ready = [&]() -> bool {
+      const bool ok = __all_sync(0xffffffffu, wait(done + g, dph));
+      if (!ok) return false;
+      dph ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      return true;
+    };
+
+    // sign flip of round rnd of repeat rr, H_8, split and operand store of
+    // chunk c (4 vectors) from x
+    auto prepare = [&](int rr, int rnd, int c, const float (&x)[32]) {
+      // signs of elements 8 i .. 8 i + 7 (bit set: +1)
+      const uint32_t sw = __ldg(a.signs + (size_t)(rr * 3 + rnd) * 32 + (row >> 2)) >> ((row & 3) * 8);
+      const float2 m1 = make_float2(-1.0f, -1.0f);
+#pragma unroll
+      for (int vv = 0; vv < 4; ++vv) {
+        float y[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          y[j] = __uint_as_float(__float_as_uint(x[8 * vv + j]) ^ ((~sw << (31 - j)) & 0x80000000u));
+        // H_8 along the row (natural order). The three butterfly stages
+        // commute; strides 4 and 2 run on packed pairs (u - v as fma(v, -1, u),
+        // exactly rounded like a subtraction), stride 1 on scalars.
+        const float2 a0 = make_float2(y[0], y[1]), a1 = make_float2(y[2], y[3]);
+        const float2 b0 = make_float2(y[4], y[5]), b1 = make_float2(y[6], y[7]);
+        const float2 s0 = __fadd2_rn(a0, b0), d0 = __ffma2_rn(b0, m1, a0);  // z0 z1 | z4 z5
+        const float2 s1 = __fadd2_rn(a1, b1), d1 = __ffma2_rn(b1, m1, a1);  // z2 z3 | z6 z7
+        const float2 t0 = __fadd2_rn(s0, s1), t1 = __ffma2_rn(s1, m1, s0);  // w0 w1 | w2 w3
+        const float2 t2 = __fadd2_rn(d0, d1), t3 = __ffma2_rn(d1, m1, d0);  // w4 w5 | w6 w7
+        const float2 w[4] = {t0, t1, t2, t3};
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+          const float2 v2 = make_float2(w[p].x + w[p].y, w[p].x - w[p].y);
+          hi[p] = bf16x2(v2.x, v2.y);
+          const float2 h2 = make_float2(__uint_as_float(hi[p] << 16), __uint_as_float(hi[p] & 0xffff0000u));
+          const float2 r2 = __ffma2_rn(h2, m1, v2);  // the remainders v - hi
+          lo[p] = bf16x2(r2.x, r2.y);
+        }
+        // column n = 8 (8 ch + 4 c + vv) + j of K rows i (hi) and 128 + i (lo)
+        unsigned char* pb = sm + kOffB + (uint32_t)g * kBBytes + (uint32_t)(8 * ch + 4 * c + vv) * kBGroupN +
+                            (uint32_t)(row & 7) * 16 + (uint32_t)(row >> 3) * kBGroupK;
+        *reinterpret_cast<uint4*>(pb) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(pb + 16 * kBGroupK) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    };
+
+    bool ok = true;
+    for (long t0 = 2L * blockIdx.x; t0 < n_tiles && ok; t0 += 2L * gridDim.x) {
+      const long tile = g == 0 ? t0 : (t0 + 1 < n_tiles ? t0 + 1 : -1);
+      stage(tile);
+      for (int st = 0; st < steps && ok; ++st) {
+        const int rr = st / 3, rnd = st % 3;
+        float2 thb[8];
+        if (st > 0) {
+          if (rnd == 0) bounds(rr - 1, thb);  // in flight during the wait
+          ok = ready();
+          if (!ok) break;
+        }
+#pragma unroll 1
+        for (int c = 0; c < 2; ++c) {
+          float x[32];
+          if (st > 0) {
+            tmem_ld32(my_tmem(c), x);
+            if (rnd == 0) output(tile, 8 * ch + 4 * c, rr - 1, x, thb);
+          }
+          if (rnd == 0) tmem_ld32(my_input(c), x);
+          prepare(rr, rnd, c, x);
+        }
+        // the operand is visible to the tensor core, and this thread's reads
+        // of the accumulator are complete, before the warp's arrival
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (l == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(full + g)) : "memory");
+      }
+      if (ok) {
+        float2 thb[8];
+        bounds(R - 1, thb);
+        ok = ready();
+        if (ok) {
+#pragma unroll 1
+          for (int c = 0; c < 2; ++c) {
+            float x[32];
+            tmem_ld32(my_tmem(c), x);
+            output(tile, 8 * ch + 4 * c, R - 1, x, thb);
           }
         }
       }
     }
-  };
-
-  // this thread's input values of slot s's tile (4 vectors x 8, zero past
-  // ldx and n_rows), staged in tensor memory for the tile's repeats
-  auto stage = [&](int s, long tile) {
-    float x[32];
-    // (ldx is a multiple of 8, so a row's 8 values are all inside or all past it)
-#pragma unroll
-    for (int vv = 0; vv < 4; ++vv) {
-      long rid;
-      const float* src = vec_src(tile, 4 * cg + vv, rid);
-      float4 u0 = make_float4(0.f, 0.f, 0.f, 0.f), u1 = u0;
-      if (src != nullptr && row * 8 < a.ldx) {
-        u0 = __ldg(reinterpret_cast<const float4*>(src + row * 8));
-        u1 = __ldg(reinterpret_cast<const float4*>(src + row * 8 + 4));
-      }
-      x[8 * vv + 0] = u0.x;
-      x[8 * vv + 1] = u0.y;
-      x[8 * vv + 2] = u0.z;
-      x[8 * vv + 3] = u0.w;
-      x[8 * vv + 4] = u1.x;
-      x[8 * vv + 5] = u1.y;
-      x[8 * vv + 6] = u1.z;
-      x[8 * vv + 7] = u1.w;
-    }
-    tmem_st32(my_input(s), x);
-  };
-
-  // One step of slot s (tile `tile`): the previous product's result (or the
-  // staged input), sign flip of round `rnd` of repeat `rr`, H_8, split,
-  // operand store; then the product. Returns false (for every thread) when a
-  // wait gave up.
-  auto step = [&](int s, long tile, int st) -> bool {
-    float x[32];
-    const int rr = st / 3, rnd = st % 3;
-    bool ok = true;
-    if (st > 0) {
-      ok = bar_wait(su32(bar + s), phase[s]);
-      if (ok) phase[s] ^= 1u;  // a product still pending keeps its parity
-      pending[s] = !ok;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      tmem_ld32(my_tmem(s), x);
-      if (rnd == 0 && ok) output(tile, rr - 1, x);
-    }
-    if (rnd == 0) tmem_ld32(my_input(s), x);
-    // signs of elements 8 i .. 8 i + 7 (bit set: +1)
-    const uint32_t sw = __ldg(a.signs + (size_t)(rr * 3 + rnd) * 32 + (row >> 2)) >> ((row & 3) * 8);
-#pragma unroll
-    for (int vv = 0; vv < 4; ++vv) {
-      float y[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        y[j] = __uint_as_float(__float_as_uint(x[8 * vv + j]) ^ ((~sw << (31 - j)) & 0x80000000u));
-      // H_8 along the row (natural order)
-#pragma unroll
-      for (int h = 1; h < 8; h <<= 1) {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if (j & h) continue;
-          const float u = y[j], v = y[j + h];
-          y[j] = u + v;
-          y[j + h] = u - v;
-        }
-      }
-      uint32_t hi[4], lo[4];
-#pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        hi[p] = bf16x2(y[2 * p], y[2 * p + 1]);
-        const float h0 = __uint_as_float(hi[p] << 16), h1 = __uint_as_float(hi[p] & 0xffff0000u);
-        lo[p] = bf16x2(y[2 * p] - h0, y[2 * p + 1] - h1);
-      }
-      // column n = 8 (4 cg + vv) + j of K rows i (hi) and 128 + i (lo)
-      unsigned char* pb = sm + kOffB + (uint32_t)s * kBBytes + (uint32_t)(4 * cg + vv) * kBGroupN +
-                          (uint32_t)(row & 7) * 16 + (uint32_t)(row >> 3) * kBGroupK;
-      *reinterpret_cast<uint4*>(pb) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-      *reinterpret_cast<uint4*>(pb + 16 * kBGroupK) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    if (__syncthreads_or(!ok)) return false;
-    if (t == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t d = tmem + (uint32_t)(s * kT5N);
-      const uint32_t b0 = su32(sm + kOffB + (uint32_t)s * kBBytes);
-#pragma unroll
-      for (int kk = 0; kk < kT5K / 16; ++kk) {
-        const uint64_t da = smem_desc(su32(sA) + kk * 2 * kALbo, kALbo, kASbo);
-        const uint64_t db = smem_desc(b0 + kk * 2 * kBGroupK, kBGroupK, kBGroupN);
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-            "l"(da), "l"(db), "r"(kIdesc), "r"(kk)
-            : "memory");
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       su32(bar + s))
-                   : "memory");
-    }
-    pending[s] = true;
-    return true;
-  };
-
-  // the last repeat's outputs of slot s
-  auto finish = [&](int s, long tile) -> bool {
-    float x[32];
-    const bool ok = bar_wait(su32(bar + s), phase[s]);
-    if (ok) phase[s] ^= 1u;
-    pending[s] = !ok;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    tmem_ld32(my_tmem(s), x);
-    if (ok) output(tile, R - 1, x);
-    return !__syncthreads_or(!ok);
-  };
-
-  for (long t0 = 2L * blockIdx.x; t0 < n_tiles && !fault; t0 += 2L * gridDim.x) {
-    const long tl[2] = {t0, t0 + 1 < n_tiles ? t0 + 1 : -1};
-    stage(0, tl[0]);
-    stage(1, tl[1]);
-    for (int st = 0; st < steps && !fault; ++st) {
-      for (int s = 0; s < 2; ++s) {
-        if (!step(s, tl[s], st)) {  // uniform across the CTA
-          fault = true;
-          break;
-        }
-      }
-    }
-    if (!fault) {
-      for (int s = 0; s < 2; ++s) {
-        if (!finish(s, tl[s])) {
-          fault = true;
-          break;
-        }
-      }
-    }
-    // the accumulators are read before the next pair overwrites them
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  }
-  if (fault) {
-    // let products still in flight finish (bounded) before the tensor memory
-    // is released
-    for (int s = 0; s < 2; ++s)
-      if (pending[s]) bar_wait(su32(bar + s), phase[s]);
-    if (t == 0) atomicAdd(&g_t5_faults, 1u);
+    if (!ok) *fault_flag = 1;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (w == 0) {
+  if (mma_warp) {
+    if (t == kT5Threads && *fault_flag) atomicAdd(&g_t5_faults, 1u);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
@@ -402,7 +485,7 @@ static cudaError_t launch_t5(const ProjArgs& a, int num_sms, cudaStream_t st) {
   long blocks = num_sms;  // one CTA per SM (shared memory and tensor memory)
   if (blocks > pairs) blocks = pairs;
   if (blocks < 1) blocks = 1;
-  k_project_t5<MODE><<<(unsigned)blocks, kT5Threads, kSmem, st>>>(a);
+  k_project_t5<MODE><<<(unsigned)blocks, kT5Threads + 32, kSmem, st>>>(a);
   return cudaGetLastError();
 }
 

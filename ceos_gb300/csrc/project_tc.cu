@@ -293,9 +293,11 @@ bool project_tc_supported(int L) { return L == 8 || L == 10; }
 cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, cudaStream_t st) {
   if (a.n_rows <= 0) return cudaSuccess;
   if (L == 10) {
+    // fhtDim 1024 runs on tcgen05 (project_t5.cu); CEOS_GB300_T5=0 selects
+    // the warp-level form below (1.3x slower at 100k x 960)
     static const bool t5 = [] {
       const char* e = std::getenv("CEOS_GB300_T5");
-      return e && e[0] == '1';
+      return !(e && e[0] == '0');
     }();
     if (t5) return launch_project_t5(a, mode, st, num_sms);
     switch (mode) {
