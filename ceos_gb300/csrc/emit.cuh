@@ -32,4 +32,24 @@ CEOS_DEV void emit_exact(const ProjArgs& a, int col, float v, int id) {
   }
 }
 
+// emit_exact for a value that passed the prefilter with the float bounds b
+// of its column: for a finite nonzero v the float tests are exact (the bounds
+// are the floats of the threshold keys themselves, see key_lower_bound), so
+// only zeros (-0 ranks below +0) and infinities read the keys.
+CEOS_DEV void emit_exact_b(const ProjArgs& a, int col, float v, int id, float2 b) {
+  if (!(v != 0.0f && isfinite(v))) {
+    emit_exact(a, col, v, id);
+    return;
+  }
+  if (a.col_active && !a.col_active[col]) return;
+  if (v >= b.x) {
+    const unsigned pos = atomicAdd(&a.cnt[2 * col], 1u);
+    if (pos < (unsigned)a.cap) a.cand[((long)2 * col) * a.cap + pos] = pack_key(v, id);
+  }
+  if (v <= b.y) {
+    const unsigned pos = atomicAdd(&a.cnt[2 * col + 1], 1u);
+    if (pos < (unsigned)a.cap) a.cand[((long)2 * col + 1) * a.cap + pos] = pack_key(-v, id);
+  }
+}
+
 }  // namespace ceos

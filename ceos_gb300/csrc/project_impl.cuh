@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(256, RegRow<L>::ok ? 3 : 1) k_project(ProjArgs
               const int e = __ffs((int)hit) - 1;
               hit &= hit - 1;
               const int j = j0 + (e << o);
-              emit_exact(a, r * a.D + j, w[padj(j)], id);
+              emit_exact_b(a, r * a.D + j, w[padj(j)], id, __ldg(tb + (e << o)));
             } while (hit);
           }
         }
