@@ -7,18 +7,18 @@ oracle/refshim standing in for the Eigen / Boost headers). This script runs
 them on seeded synthetic inputs and writes their outputs:
 
 * reference_small.npz  - small cases with their inputs stored: coCEOs-Est,
-                         CEOs-Hash and CEOs-Est (dense) on config-0-shaped
+                         CEOs-Hash and CEOs-Est (dense) on Netflix-shaped (17,770 x 300)
                          data, coCEOs-Est on integer (SIFT-shaped) data with
                          exact ties, and a FIFO streamCEOs sequence; full
                          buckets and search results.
-* reference_c0.npz     - the full config-0 workload (17,770 x 300, D=1024,
+* reference_netflix.npz     - the full Netflix-shaped 17,770 x 300 workload (17,770 x 300, D=1024,
                          R=2, m=100, s=20, c=500, k=10, 1,000 queries, index
                          seed 42): search results of all three methods,
                          checksums of the bucket values and 64 sampled
                          columns. Inputs are regenerated from their seeds;
                          their sha256 is stored so a test can tell a changed
                          generator from a changed result.
-* reference_stream.npz - a config-4-shaped FIFO stream (rows as config 0,
+* reference_stream.npz - a FIFO stream shaped like the streaming benchmark (rows as the Netflix-shaped workload,
                          d=300, D=1024, R=4, m=200, p=m as the reference's
                          scripts set it) with a reduced start of 60,000 rows
                          and three update calls; per step the search results
@@ -43,16 +43,16 @@ from oracle import reference as REF  # noqa: E402
 from parity import sha256  # noqa: E402
 
 # Workload definitions shared with the tests that read these fixtures.
-C0 = dict(n=17770, d=300, nq=1000, D=1024, R=2, m=100, s=20, c=500, k=10, seed=42,
+NETFLIX = dict(n=17770, d=300, nq=1000, D=1024, R=2, m=100, s=20, c=500, k=10, seed=42,
           x_seed=1770, q_seed=300)
 STREAM = dict(n0=60000, d=300, nq=100, D=1024, R=4, m=200, s=20, c=500, k=10, seed=42,
               x_seed=4242, q_seed=4343, steps=((20000, 6000), (15000, 3000), (5000, 1000)))
 SAMPLED_COLUMNS = 64
 
 
-def c0_inputs():
-    return (netflix_like(C0["n"], C0["d"], seed=C0["x_seed"]),
-            gaussian_queries(C0["nq"], C0["d"], seed=C0["q_seed"]))
+def netflix_inputs():
+    return (netflix_like(NETFLIX["n"], NETFLIX["d"], seed=NETFLIX["x_seed"]),
+            gaussian_queries(NETFLIX["nq"], NETFLIX["d"], seed=NETFLIX["q_seed"]))
 
 
 def stream_inputs():
@@ -78,7 +78,7 @@ def lists_full(ids: np.ndarray, live: int) -> bool:
 
 def small_cases(out):
     rng = np.random.default_rng(20240315)
-    # config-0-shaped: coCEOs-Est, CEOs-Hash, dense CEOs-Est
+    # Netflix-shaped (17,770 x 300): coCEOs-Est, CEOs-Hash, dense CEOs-Est
     n, d, nq = 900, 44, 40
     X = (rng.standard_normal((n, d)) / np.sqrt(d) * rng.lognormal(0, 0.5, (n, 1))).astype(np.float32)
     Q = rng.standard_normal((nq, d)).astype(np.float32)
@@ -130,19 +130,19 @@ def small_cases(out):
         out[f"stream_{i}_hash_ids"], out[f"stream_{i}_hash_dists"] = st.hash_search(Qt, 10)
 
 
-def c0_case(out):
-    X, Q = c0_inputs()
+def netflix_case(out):
+    X, Q = netflix_inputs()
     out["x_sha256"], out["q_sha256"] = np.array(sha256(X)), np.array(sha256(Q))
-    cols = sampled_columns(C0["D"] * C0["R"])
+    cols = sampled_columns(NETFLIX["D"] * NETFLIX["R"])
     out["columns"] = cols
     for kind, b, srch in (("coceos", "build_coCEOs_Est", "search_coCEOs_Est"),
                           ("hash", "build_CEOs_Hash", "search_CEOs_Hash"),
                           ("dense", "build", "search")):
-        r = REF.RefCEOs(C0["n"], C0["d"])
-        r.setIndexParam(C0["D"], C0["R"], C0["m"], 8, C0["seed"])
+        r = REF.RefCEOs(NETFLIX["n"], NETFLIX["d"])
+        r.setIndexParam(NETFLIX["D"], NETFLIX["R"], NETFLIX["m"], 8, NETFLIX["seed"])
         getattr(r, b)(X)
-        r.n_probed_vectors, r.n_cand = C0["s"], C0["c"]
-        out[f"{kind}_ids"], out[f"{kind}_dists"] = getattr(r, srch)(Q, C0["k"])
+        r.n_probed_vectors, r.n_cand = NETFLIX["s"], NETFLIX["c"]
+        out[f"{kind}_ids"], out[f"{kind}_dists"] = getattr(r, srch)(Q, NETFLIX["k"])
         if kind == "coceos":
             bi, bv = r.buckets()
             out["bucket_vals_sha256"] = np.array(sha256(bv))
@@ -177,7 +177,7 @@ def stream_case(out):
 def main():
     if not REF.available():
         raise SystemExit("the reference library could not be built here")
-    for name, fn in (("reference_small.npz", small_cases), ("reference_c0.npz", c0_case),
+    for name, fn in (("reference_small.npz", small_cases), ("reference_netflix.npz", netflix_case),
                      ("reference_stream.npz", stream_case)):
         out = {}
         fn(out)

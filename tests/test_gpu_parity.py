@@ -40,7 +40,7 @@ def build_pair(gpu, oracle, X, D, R, m, seed, kind="coceos"):
 
 
 @pytest.mark.parametrize("n,d,D,R", [
-    (200, 300, 1024, 2),   # config-0 shape: F = 1024
+    (200, 300, 1024, 2),   # the Netflix-shaped workload: F = 1024
     (300, 128, 256, 3),    # F = 256
     (257, 150, 256, 2),    # row padding (150 -> 152)
     (100, 5, 4, 2),        # F = 8
@@ -398,7 +398,7 @@ def test_bruteforce_fp64_matches_oracle(gpu, oracle, n, d, k, kind):
 
 
 @pytest.mark.gpu
-def test_config0_full_size_parity(gpu, oracle):
+def test_netflix_workload_full_size_parity(gpu, oracle):
     """The CPU-runnable configuration at full size: 17,770 x 300 rows g*s
     (g ~ N(0, I/300), s ~ LogNormal(0, 0.5)), 1000 N(0, I) queries, n_proj 1024,
     n_repeats 2, top_m 100, n_probed_vectors 20, n_cand 500, k 10, seed 42:

@@ -3,7 +3,7 @@
 It carries the reference's module name and bindings (python/python_wrapper.cpp
 :13-74): the same classes, constructor arguments, setIndexParam keywords and
 defaults, read/write attributes and methods. The CPU tests check that surface
-and that there is no CPU path; the GPU test runs the full config-0 workload
+and that there is no CPU path; the GPU test runs the full Netflix-shaped 17,770 x 300 workload
 through `import CEOs` against the committed outputs of the reference's own
 code.
 """
@@ -108,33 +108,33 @@ def test_no_cpu_path(CEOs):
 
 
 @pytest.mark.gpu
-def test_config0_through_import_CEOs(gpu, CEOs):
-    """The full config-0 workload through `import CEOs`, checked against the
+def test_netflix_workload_through_import_CEOs(gpu, CEOs):
+    """The full Netflix-shaped 17,770 x 300 workload through `import CEOs`, checked against the
     reference's own outputs and bit for bit against the ctypes module."""
-    from golden.make_reference_golden import C0, c0_inputs
+    from golden.make_reference_golden import NETFLIX, netflix_inputs
     from parity import compare_results
 
-    f = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_c0.npz"))
-    X, Q = c0_inputs()
+    f = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_netflix.npz"))
+    X, Q = netflix_inputs()
     for kind, b, srch in (("coceos", "build_coCEOs_Est", "search_coCEOs_Est"),
                           ("hash", "build_CEOs_Hash", "search_CEOs_Hash"),
                           ("dense", "build", "search")):
-        idx = CEOs.CEOs(C0["n"], C0["d"])
-        idx.setIndexParam(C0["D"], C0["R"], C0["m"], 8, C0["seed"])
+        idx = CEOs.CEOs(NETFLIX["n"], NETFLIX["d"])
+        idx.setIndexParam(NETFLIX["D"], NETFLIX["R"], NETFLIX["m"], 8, NETFLIX["seed"])
         getattr(idx, b)(X.astype(np.float64))  # another dtype: converted like the reference's Ref
-        idx.n_probed_vectors, idx.n_cand = C0["s"], C0["c"]
-        ids, dists = getattr(idx, srch)(Q, C0["k"])
-        assert ids.dtype == np.int32 and dists.dtype == np.float32 and ids.shape == (C0["nq"], C0["k"])
+        idx.n_probed_vectors, idx.n_cand = NETFLIX["s"], NETFLIX["c"]
+        ids, dists = getattr(idx, srch)(Q, NETFLIX["k"])
+        assert ids.dtype == np.int32 and dists.dtype == np.float32 and ids.shape == (NETFLIX["nq"], NETFLIX["k"])
         ok, stats = compare_results(ids, dists, f[f"{kind}_ids"], f[f"{kind}_dists"])
         assert ok, (kind, stats)
-        g = gpu.CEOs(C0["n"], C0["d"])
-        g.setIndexParam(C0["D"], C0["R"], C0["m"], 8, C0["seed"])
+        g = gpu.CEOs(NETFLIX["n"], NETFLIX["d"])
+        g.setIndexParam(NETFLIX["D"], NETFLIX["R"], NETFLIX["m"], 8, NETFLIX["seed"])
         getattr(g, b)(X)
-        g.n_probed_vectors, g.n_cand = C0["s"], C0["c"]
-        gi, gd = getattr(g, srch)(Q, C0["k"])
+        g.n_probed_vectors, g.n_cand = NETFLIX["s"], NETFLIX["c"]
+        gi, gd = getattr(g, srch)(Q, NETFLIX["k"])
         assert np.array_equal(gi, ids) and np.array_equal(gd.view(np.uint32), dists.view(np.uint32))
     # streamCEOs through the module, and the reference's error path
-    st = CEOs.streamCEOs(C0["d"])
+    st = CEOs.streamCEOs(NETFLIX["d"])
     st.setIndexParam(256, 2, 50, 1, 7)
     st.build(X[:5000])
     st.update(X[5000:6000], 500)

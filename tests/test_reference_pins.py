@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 from conftest import gaussian_queries, gist_like, netflix_like, sift_like
-from golden.make_reference_golden import C0, STREAM, c0_inputs, stream_inputs
+from golden.make_reference_golden import NETFLIX, STREAM, netflix_inputs, stream_inputs
 from parity import compare_buckets, compare_results, sha256
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -89,10 +89,10 @@ def run_small(impl):
                        f"stream hash {i}")
 
 
-def run_c0(impl):
-    """The full config-0 workload: 17,770 x 300, 1,000 queries."""
-    f = _load("reference_c0.npz")
-    X, Q = c0_inputs()
+def run_netflix(impl):
+    """The full Netflix-shaped 17,770 x 300 workload: 17,770 x 300, 1,000 queries."""
+    f = _load("reference_netflix.npz")
+    X, Q = netflix_inputs()
     assert sha256(X) == str(f["x_sha256"]) and sha256(Q) == str(f["q_sha256"]), \
         "the seeded input generator differs from the one the fixture was made with"
     cols = f["columns"]
@@ -100,8 +100,8 @@ def run_c0(impl):
     for kind, b, srch in (("coceos", "build_coCEOs_Est", "search_coCEOs_Est"),
                           ("hash", "build_CEOs_Hash", "search_CEOs_Hash"),
                           ("dense", "build", "search")):
-        idx = impl.CEOs(C0["n"], C0["d"])
-        idx.setIndexParam(C0["D"], C0["R"], C0["m"], 8, C0["seed"])
+        idx = impl.CEOs(NETFLIX["n"], NETFLIX["d"])
+        idx.setIndexParam(NETFLIX["D"], NETFLIX["R"], NETFLIX["m"], 8, NETFLIX["seed"])
         getattr(idx, b)(X)
         if kind == "coceos":
             bi, bv = idx.buckets()
@@ -111,14 +111,14 @@ def run_c0(impl):
             bi, _ = idx.buckets()
             v = f["bucket_vals_sampled"]
             _check_buckets((bi[cols], v), f["hash_bucket_ids_sampled"], v, kind)
-        idx.n_probed_vectors, idx.n_cand = C0["s"], C0["c"]
-        stats[kind] = _check_results(getattr(idx, srch)(Q, C0["k"]), (f[f"{kind}_ids"], f[f"{kind}_dists"]),
+        idx.n_probed_vectors, idx.n_cand = NETFLIX["s"], NETFLIX["c"]
+        stats[kind] = _check_results(getattr(idx, srch)(Q, NETFLIX["k"]), (f[f"{kind}_ids"], f[f"{kind}_dists"]),
                                      kind)
     return stats
 
 
 def run_stream(impl):
-    """Config-4-shaped FIFO stream: 60,000 x 300 start, three updates."""
+    """FIFO stream shaped like the streaming benchmark: 60,000 x 300 start, three updates."""
     f = _load("reference_stream.npz")
     X, Q = stream_inputs()
     assert sha256(X) == str(f["x_sha256"]) and sha256(Q) == str(f["q_sha256"]), \
@@ -150,8 +150,8 @@ def test_oracle_matches_reference_small(oracle):
     run_small(oracle)
 
 
-def test_oracle_matches_reference_config0(oracle):
-    run_c0(oracle)
+def test_oracle_matches_reference_netflix(oracle):
+    run_netflix(oracle)
 
 
 def test_oracle_matches_reference_stream(oracle):
@@ -199,8 +199,8 @@ def test_gpu_matches_reference_small(gpu):
 
 
 @pytest.mark.gpu
-def test_gpu_matches_reference_config0(gpu):
-    run_c0(gpu)
+def test_gpu_matches_reference_netflix(gpu):
+    run_netflix(gpu)
 
 
 @pytest.mark.gpu
