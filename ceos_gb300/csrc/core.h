@@ -367,6 +367,13 @@ struct Core {
     a.row_map = exact ? nullptr : rowmap.as<long>();
     a.n_rows = S;
     a.out = samp.as<float>();  // row-major [S][C]
+    // A sample of a split-precision index is projected by the FP32 kernel,
+    // which splits few rows finer over the SMs than the tensor-core tiles: its
+    // thresholds only filter the candidates (the float tests below compare
+    // split-precision values with them), and a column end that comes up short
+    // is selected exactly from the split-precision projection. An exact
+    // sample (S == n) keeps the index's own precision.
+    if (!exact) a.tensor = 0;
     CUDA_TRY(launch_project(a, PROJ_ROWS, L, sms, stream));
     CUDA_TRY(th.ensure((size_t)Cc * 2 * 4));
     CUDA_TRY(thf.ensure((size_t)Cc * sizeof(float2)));
@@ -388,17 +395,20 @@ struct Core {
     e.cap = (int)cap;
     CUDA_TRY(launch_project(e, PROJ_EMIT, L, sms, stream));
     timer.mark("project+emit");
-    if (e.tensor && L == 10) {
-      // the tensor-core projection ends a CTA whose bounded wait gave up
-      const int faults = project_t5_take_faults(stream);
-      if (faults != 0)
-        return fail(CEOS_ERR_CUDA, "tensor-core projection: %d blocks stopped at a wait that did not complete", faults);
-    }
     CUDA_TRY(dBids.ensure((size_t)Cc * 2 * m * 4));
     CUDA_TRY(dBvals.ensure((size_t)Cc * 2 * m * 4));
     CUDA_TRY(launch_finish_buckets(cand.as<uint64_t>(), cnt.as<unsigned>(), (int)cap, Cc, m,
                                    dBids.as<int>(), dBvals.as<float>(), failb.as<unsigned>(), stream));
     timer.mark("select");
+    if (e.tensor && L == 10) {
+      // The tensor-core projection ends a CTA whose bounded wait gave up. The
+      // count is read after the selection is queued (the selection only reads
+      // the candidate lists within their counts and capacity), so the device
+      // runs on without a host round trip; on a fault the index is released.
+      const int faults = project_t5_take_faults(stream);
+      if (faults != 0)
+        return fail(CEOS_ERR_CUDA, "tensor-core projection: %d blocks stopped at a wait that did not complete", faults);
+    }
     samp.release();
     cand.release();
     // ---- exact fallback for flagged column ends ----

@@ -34,6 +34,11 @@
 // Every wait is bounded and also gives up once the other side has recorded a
 // fault; the fault (read by project_t5_take_faults) ends the CTA after a
 // bounded wait for its products in flight, and the tensor memory is freed.
+//
+// Candidate emission (PROJ_EMIT): on an output step each warp gathers its
+// flagged values in a shared-memory list, one value per lane and pass, and
+// appends the list to the global candidate lists after its arrival, one
+// entry per lane, while the tensor core multiplies its next operand.
 #include "kernels.h"
 #include "common.cuh"
 #include "emit.cuh"
@@ -43,24 +48,33 @@ namespace ceos {
 namespace {
 
 constexpr int kT5Threads = 512;  // compute threads; one more warp issues the products
-constexpr int kT5Vec = 16;         // vectors per tile
-constexpr int kT5N = kT5Vec * 8;   // accumulator columns per tile
+// tiles in flight, one per compute group (four tiles of 8 vectors, N = 64,
+// ran slower: twice the products per vector)
+constexpr int kSlots = 2;
+constexpr int kGroupWarps = kT5Threads / 32 / kSlots;
+constexpr int kT5Vec = 32 / kSlots;            // vectors per tile
+constexpr int kT5N = kT5Vec * 8;               // accumulator columns per tile
 constexpr int kT5K = 256;          // hi and lo rows of the 128-row operand
 // A = [H | H]: M = 128 x K = 256 bfloat16, K-major core matrices (8 rows of 16
 // bytes along K), 8-K groups 128 bytes apart, 8-row groups 4096 bytes apart
 constexpr uint32_t kALbo = 128;
 constexpr uint32_t kASbo = 4096;
 constexpr uint32_t kABytes = 128 * kT5K * 2;
-// B = W: N = 128 x K = 256 bfloat16, MN-major core matrices (8 columns of 16
-// bytes along N), 8-column groups 128 bytes apart, 8-K groups 2048 bytes apart
+// B = W: N x K = 256 bfloat16, MN-major core matrices (8 columns of 16 bytes
+// along N), 8-column groups 128 bytes apart, 8-K groups N x 16 bytes apart
 constexpr uint32_t kBGroupN = 128;
-constexpr uint32_t kBGroupK = 2048;
+constexpr uint32_t kBGroupK = kT5N * 16;
 constexpr uint32_t kBBytes = kT5N * kT5K * 2;
 constexpr uint32_t kOffA = 0;
-constexpr uint32_t kOffB = kOffA + kABytes;        // two operand buffers
-constexpr uint32_t kOffBar = kOffB + 2 * kBBytes;  // four mbarriers, tmem holder, fault flag
-constexpr uint32_t kSmem = kOffBar + 64;
-constexpr int kTmemCols = 4 * kT5N;  // accumulators, then staged inputs
+constexpr uint32_t kOffB = kOffA + kABytes;             // one operand buffer per slot
+constexpr uint32_t kOffBar = kOffB + kSlots * kBBytes;  // mbarriers, tmem holder, fault flag
+// per compute warp, the candidates of an output step: kList (value, id)
+// pairs, then their lists (2 column + end)
+constexpr int kList = 64;
+constexpr uint32_t kListBytes = kList * 12;
+constexpr uint32_t kOffList = kOffBar + 128;
+constexpr uint32_t kSmem = kOffList + (kT5Threads / 32) * kListBytes;
+constexpr int kTmemCols = 2 * kSlots * kT5N;  // accumulators, then staged inputs
 // Instruction descriptor (kind::f16): D FP32 (bits 4-5 = 1), A and B
 // bfloat16 (bits 7-9, 10-12 = 1), A K-major (bit 15 = 0), B MN-major (bit 16),
 // N >> 3 at bits 17-22, M >> 4 at bits 24-28.
@@ -120,24 +134,26 @@ CEOS_DEV uint32_t bf16x2(float lo, float hi) {
 
 }  // namespace
 
+// 17 warps: five of them share one of the SM's four 16,384-register
+// partitions, so a thread has at most 96 registers.
 template <int MODE>
 __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const int t = threadIdx.x, w = t >> 5, l = t & 31;
   const bool mma_warp = w == kT5Threads / 32;  // the last warp issues the products
-  // compute warp w serves slot g = w / 8; within its group it owns lane
-  // quarter q of the tensor memory and column half ch (vectors 8 ch .. 8 ch + 7)
-  const int g = (w >> 3) & 1;
+  // compute warp w serves slot g = w / kGroupWarps; within its group it owns
+  // lane quarter q of the tensor memory and vectors 8 ch .. 8 ch + 7
+  const int g = (w / kGroupWarps) % kSlots;
   const int q = w & 3;
-  const int ch = (w >> 2) & 1;
+  const int ch = (w >> 2) % (kGroupWarps / 4);
   const int row = 32 * q + l;   // the row i of X (and lane of the accumulator)
   unsigned char* sA = sm + kOffA;
   // full[s]: slot s's operand is written (one arrival per compute warp);
   // done[s]: slot s's product has completed (tcgen05.commit)
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + kOffBar);
-  uint64_t* done = full + 2;
-  uint32_t* holder = reinterpret_cast<uint32_t*>(sm + kOffBar + 32);
-  volatile int* fault_flag = reinterpret_cast<volatile int*>(sm + kOffBar + 36);
+  uint64_t* done = full + kSlots;
+  uint32_t* holder = reinterpret_cast<uint32_t*>(sm + kOffBar + 96);
+  volatile int* fault_flag = reinterpret_cast<volatile int*>(sm + kOffBar + 100);
   const int R = a.R, D = a.D, C = a.R * a.D;
 
   // A = [H | H]: element (m, k) = (-1)^popc(m & (k mod 128))
@@ -158,8 +174,8 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
     *reinterpret_cast<uint4*>(sA + (m & 7) * 16 + (m >> 3) * kASbo + kg * kALbo) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
   }
   if (t == 0) {
-    for (int s = 0; s < 2; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(full + s)), "r"(kT5Threads / 64) : "memory");
+    for (int s = 0; s < kSlots; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(full + s)), "r"(kGroupWarps) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(done + s)) : "memory");
     }
     *fault_flag = 0;
@@ -200,16 +216,20 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
 
   if (mma_warp) {
     // ---- the product issuer: one elected lane ----
-    uint32_t fph[2] = {0u, 0u};
-    int issued[2] = {0, 0};  // commits per slot
+    uint32_t fph = 0u;  // bit s: phase of full[s]
+    int issued[kSlots];  // commits per slot
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) issued[s] = 0;
     bool ok = true;
-    for (long t0 = 2L * blockIdx.x; t0 < n_tiles && ok; t0 += 2L * gridDim.x) {
+    for (long t0 = (long)kSlots * blockIdx.x; t0 < n_tiles && ok; t0 += (long)kSlots * gridDim.x) {
       for (int st = 0; st < steps && ok; ++st) {
-        for (int s = 0; s < 2 && ok; ++s) {
-          ok = wait(full + s, fph[s]);
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s) {
+          if (!ok) break;
+          ok = wait(full + s, (fph >> s) & 1u);
           ok = __all_sync(0xffffffffu, ok);
           if (!ok) break;
-          fph[s] ^= 1u;
+          fph ^= 1u << s;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           if (l == 0) {
             const uint32_t d = tmem + (uint32_t)(s * kT5N);
@@ -236,7 +256,8 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
     if (!ok) {
       // products still in flight finish (bounded) before the tensor memory
       // is released: wait for every commit of each slot
-      for (int s = 0; s < 2; ++s) {
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s) {
         if (issued[s] == 0) continue;
         const uint32_t last = (uint32_t)((issued[s] - 1) & 1);
         for (int it = 0; it < (1 << 16); ++it) {
@@ -256,7 +277,7 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
     // this thread's lane quarter and its 32 columns of chunk c (vectors
     // 8 ch + 4 c .. + 3) of the accumulator, and of the staged input rows
     auto my_tmem = [&](int c) { return tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * kT5N + 64 * ch + 32 * c); };
-    auto my_input = [&](int c) { return my_tmem(c) + (uint32_t)(2 * kT5N); };
+    auto my_input = [&](int c) { return my_tmem(c) + (uint32_t)(kSlots * kT5N); };
     uint32_t dph = 0u;
 
     // row pointer of vector v (0..15) of tile `tile`, null past n_rows
@@ -270,6 +291,26 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
       return a.X + src * a.ldx;
     };
 
+    // The warp's candidate list (PROJ_EMIT): output steps append their
+    // flagged values to it in shared memory, and flush() appends the list to
+    // the global candidate lists, one entry per lane, so that a step waits for
+    // one round of global atomics however its flagged values fall on lanes.
+    float2* lval = reinterpret_cast<float2*>(sm + kOffList + (uint32_t)w * kListBytes);  // (v, id bits)
+    uint32_t* lend = reinterpret_cast<uint32_t*>(lval + kList);
+    int lcount = 0;  // entries in the list (the same in every lane)
+    auto flush = [&]() {
+      __syncwarp();
+      for (int i = l; i < lcount; i += 32) {
+        const uint32_t ce = lend[i];
+        const float2 e = lval[i];
+        const unsigned pos = atomicAdd(&a.cnt[ce], 1u);
+        if (pos < (unsigned)a.cap)
+          a.cand[(long)ce * a.cap + pos] = pack_key((ce & 1u) ? -e.x : e.x, __float_as_int(e.y));
+      }
+      __syncwarp();
+      lcount = 0;
+    };
+
     // outputs of repeat rr held in x (this thread's row of vectors v0 .. v0 + 3);
     // thb: the float bounds of the 8 output columns (PROJ_EMIT)
     auto output = [&](long tile, int v0, int rr, const float (&x)[32], const float2 (&thb)[8]) {
@@ -279,43 +320,64 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
         uint32_t hit = 0;
 #pragma unroll
         for (int e = 0; e < 32; ++e)
-          if (idx0 + (e & 7) < D && emit_maybe(x[e], thb[e & 7])) hit |= 1u << e;
-        // the few flagged values, one at a time (the loop stays rolled: every
-        // warp of the SM shares the instruction cache)
+          if (emit_maybe(x[e], thb[e & 7])) hit |= 1u << e;
+        // only output indices below D, and vectors below n_rows
+        const int nj = min(8, max(0, D - idx0));
+        const int nv = tile < 0 ? 0 : (int)min(4L, max(0L, a.n_rows - (tile * kT5Vec + v0)));
+        const uint32_t jm = (1u << nj) - 1u;
+        hit &= (jm | (jm << 8) | (jm << 16) | (jm << 24)) & (nv >= 4 ? 0xffffffffu : (1u << (8 * nv)) - 1u);
+        // the few flagged values, one per lane and pass (the loop stays
+        // rolled: every warp of the SM shares the instruction cache)
 #pragma unroll 1
-        while (hit) {
-          const int e = __ffs(hit) - 1;
-          hit &= hit - 1u;
-          const int j = e & 7;
-          long rid;
-          if (vec_src(tile, v0 + (e >> 3), rid) == nullptr) continue;
-          const int col = rr * D + idx0 + j;
-          if (a.col_active && !a.col_active[col]) continue;
-          float v = x[0];
+        while (__any_sync(0xffffffffu, hit != 0)) {
+          bool close = false, far = false;
+          int col = 0, id = 0;
+          float v = 0.0f;
+          if (hit != 0) {
+            const int e = __ffs(hit) - 1;
+            hit &= hit - 1u;
+            const int j = e & 7;
+            col = rr * D + idx0 + j;
+            if (!(a.col_active && !a.col_active[col])) {
+              v = x[0];
 #pragma unroll
-          for (int i = 1; i < 32; ++i)
-            if (i == e) v = x[i];
-          float2 bj = thb[0];
+              for (int i = 1; i < 32; ++i)
+                if (i == e) v = x[i];
+              float2 bj = thb[0];
 #pragma unroll
-          for (int i = 1; i < 8; ++i)
-            if (i == j) bj = thb[i];
-          const int id = (int)(a.id_base + (a.row_map ? a.row_map[rid] : rid));
-          // For a finite nonzero v the float bounds are exact (thb holds the
-          // floats of the threshold keys, emit_bounds); zeros (-0 ranks below
-          // +0) and infinities take the key test.
-          bool close, far;
-          if (v != 0.0f && isfinite(v)) {
-            close = v >= bj.x;
-            far = v <= bj.y;
-          } else {
-            const uint2 th = __ldg(reinterpret_cast<const uint2*>(a.th) + col);
-            close = fkey(v) >= th.x;
-            far = fkey(-v) >= th.y;
+              for (int i = 1; i < 8; ++i)
+                if (i == j) bj = thb[i];
+              const long rid = tile * kT5Vec + v0 + (e >> 3);
+              id = (int)(a.id_base + (a.row_map ? a.row_map[rid] : rid));
+              // For a finite nonzero v the float bounds are exact (thb holds
+              // the floats of the threshold keys, emit_bounds); zeros (-0 ranks
+              // below +0) and infinities take the key test.
+              if (v != 0.0f && isfinite(v)) {
+                close = v >= bj.x;
+                far = v <= bj.y;
+              } else {
+                const uint2 th = __ldg(reinterpret_cast<const uint2*>(a.th) + col);
+                close = fkey(v) >= th.x;
+                far = fkey(-v) >= th.y;
+              }
+            }
           }
-          const unsigned pc = close ? atomicAdd(&a.cnt[2 * col], 1u) : 0xffffffffu;
-          const unsigned pf = far ? atomicAdd(&a.cnt[2 * col + 1], 1u) : 0xffffffffu;
-          if (pc < (unsigned)a.cap) a.cand[(2L * col) * a.cap + pc] = pack_key(v, id);
-          if (pf < (unsigned)a.cap) a.cand[(2L * col + 1) * a.cap + pf] = pack_key(-v, id);
+          const uint32_t bc = __ballot_sync(0xffffffffu, close);
+          const uint32_t bf = __ballot_sync(0xffffffffu, far);
+          const int nnew = __popc(bc) + __popc(bf);
+          if (lcount + nnew > kList) flush();
+          const uint32_t below = (1u << l) - 1u;
+          if (close) {
+            const int p = lcount + __popc(bc & below);
+            lval[p] = make_float2(v, __int_as_float(id));
+            lend[p] = 2u * (uint32_t)col;
+          }
+          if (far) {
+            const int p = lcount + __popc(bc) + __popc(bf & below);
+            lval[p] = make_float2(v, __int_as_float(id));
+            lend[p] = 2u * (uint32_t)col + 1u;
+          }
+          lcount += nnew;
         }
       } else {
 #pragma unroll
@@ -424,8 +486,8 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
     };
 
     bool ok = true;
-    for (long t0 = 2L * blockIdx.x; t0 < n_tiles && ok; t0 += 2L * gridDim.x) {
-      const long tile = g == 0 ? t0 : (t0 + 1 < n_tiles ? t0 + 1 : -1);
+    for (long t0 = (long)kSlots * blockIdx.x; t0 < n_tiles && ok; t0 += (long)kSlots * gridDim.x) {
+      const long tile = t0 + g < n_tiles ? t0 + g : -1;
       stage(tile);
       for (int st = 0; st < steps && ok; ++st) {
         const int rr = st / 3, rnd = st % 3;
@@ -451,6 +513,8 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
         if (l == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(full + g)) : "memory");
+        // the step's candidates go out while the tensor core multiplies
+        if (MODE == PROJ_EMIT && lcount > 0) flush();
       }
       if (ok) {
         float2 thb[8];
@@ -463,6 +527,7 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
             tmem_ld32(my_tmem(c), x);
             output(tile, 8 * ch + 4 * c, R - 1, x, thb);
           }
+          if (MODE == PROJ_EMIT && lcount > 0) flush();
         }
       }
     }
@@ -481,9 +546,9 @@ template <int MODE>
 static cudaError_t launch_t5(const ProjArgs& a, int num_sms, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_project_t5<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
   if (e != cudaSuccess) return e;
-  const long pairs = (a.n_rows + 2 * kT5Vec - 1) / (2 * kT5Vec);
+  const long groups = (a.n_rows + kSlots * kT5Vec - 1) / (kSlots * kT5Vec);
   long blocks = num_sms;  // one CTA per SM (shared memory and tensor memory)
-  if (blocks > pairs) blocks = pairs;
+  if (blocks > groups) blocks = groups;
   if (blocks < 1) blocks = 1;
   k_project_t5<MODE><<<(unsigned)blocks, kT5Threads + 32, kSmem, st>>>(a);
   return cudaGetLastError();

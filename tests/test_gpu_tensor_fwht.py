@@ -74,9 +74,10 @@ def test_tensor_sampled_build_selects_exactly(gpu, d, D, R):
     """n > 65536 takes the sampled-threshold build; with the tensor-core
     projection its buckets must be exactly the two-ended top-m of the
     split-precision projections themselves. The dense build of the same index
-    produces the same projection values (column dump, row sample and fused
-    emission all run the same kernel), and the order is the library's: key of
-    the value, then the smaller id."""
+    produces the same projection values (its row projection, the column dump
+    and the fused emission run the same kernel; the threshold sample runs on
+    the FP32 kernel and only filters the candidates), and the order is the
+    library's: key of the value, then the smaller id."""
     n, m = 70000, 64
     X = netflix_like(n, d, seed=17)
     dense = gpu.CEOs(n, d)
