@@ -106,8 +106,9 @@ struct QueryArgs {
   const int* probes = nullptr;  // [nq][s] tags in pop order
   float* est = nullptr;         // [nq][n]
   int* probes_out = nullptr;
-  // sort-based estimate accumulation (k_query_sorted): per-CTA scratch of
-  // 2 x sort_cap (id, value) pairs, ids below 2^id_bits
+  // sort-based estimate accumulation (k_query_sorted): 2 x grid x sort_cap
+  // (id, value) pairs, every CTA's first buffer, then every CTA's second;
+  // ids below 2^id_bits
   int2* sort_scratch = nullptr;
   long sort_cap = 0;
   int id_bits = 0;

@@ -92,6 +92,22 @@ CEOS_DEV float dot_g8(const float* __restrict__ q, const float* __restrict__ x, 
   return s;
 }
 
+// Prefetch into L2 the rows of candidates keys[i0 .. i0 + 8) (lane l: row
+// i0 + l / 4, its 128-byte line l % 4), one step of a warp's rerank loop
+// ahead. Long candidate lists of short rows only: at 8000 candidates of 512
+// bytes per query it took 2.6% off the search, at 2000 it added 1.7%, and on
+// 3840-byte rows (4000 candidates) it cost 9%.
+constexpr int kRerankPrefetchMin = 3072;
+template <typename RowPtr>
+CEOS_DEV void prefetch_rows(const uint64_t* keys, int n, int i0, int row_bytes, RowPtr row) {
+  const int lane = threadIdx.x & 31;
+  const int i = i0 + (lane >> 2);
+  if (i >= n || row_bytes > 512) return;
+  const char* p = reinterpret_cast<const char*>(row(key_id(keys[i])));
+  for (int off = 128 * (lane & 3); off < row_bytes; off += 512)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + off));
+}
+
 // Approximate score for the split-precision scan: like dot_g8 but over
 // 8-element chunks of the bfloat16 row (16 bytes per lane per load); chunk c
 // goes to lane c mod 8, each lane a sequential FMA chain, then the butterfly.
@@ -129,7 +145,57 @@ CEOS_DEV float dot_g8_bf16(const float* __restrict__ q, const uint16_t* __restri
   return s;
 }
 
-// Split-precision rerank of keys[0..n) in place (approximate bfloat16 scores).
+// dot_g8_bf16 of one query with two rows at once (each row's sum in exactly
+// dot_g8_bf16's order): an 8-lane group keeps twice as many loads in flight.
+CEOS_DEV void dot_g8_bf16_2(const float* __restrict__ q, const uint16_t* __restrict__ xa,
+                            const uint16_t* __restrict__ xb, int n8, int g, float& sa, float& sb) {
+  const uint4* a8 = reinterpret_cast<const uint4*>(xa);
+  const uint4* b8 = reinterpret_cast<const uint4*>(xb);
+  const float4* q4 = reinterpret_cast<const float4*>(q);
+  float s0 = 0.0f, s1 = 0.0f;
+  auto acc8 = [&](float& s, const uint4 w, int c) {
+    const float4 qa = q4[2 * c], qb = q4[2 * c + 1];
+    s = __fmaf_rn(qa.x, __uint_as_float(w.x << 16), s);
+    s = __fmaf_rn(qa.y, __uint_as_float(w.x & 0xffff0000u), s);
+    s = __fmaf_rn(qa.z, __uint_as_float(w.y << 16), s);
+    s = __fmaf_rn(qa.w, __uint_as_float(w.y & 0xffff0000u), s);
+    s = __fmaf_rn(qb.x, __uint_as_float(w.z << 16), s);
+    s = __fmaf_rn(qb.y, __uint_as_float(w.z & 0xffff0000u), s);
+    s = __fmaf_rn(qb.z, __uint_as_float(w.w << 16), s);
+    s = __fmaf_rn(qb.w, __uint_as_float(w.w & 0xffff0000u), s);
+  };
+  int c = g;
+  for (; c + 24 < n8; c += 32) {
+    uint4 wa[4], wb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      wa[u] = __ldcg(a8 + c + 8 * u);
+      wb[u] = __ldcg(b8 + c + 8 * u);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      acc8(s0, wa[u], c + 8 * u);
+      acc8(s1, wb[u], c + 8 * u);
+    }
+  }
+  for (; c < n8; c += 8) {
+    const uint4 wa = __ldcg(a8 + c), wb = __ldcg(b8 + c);
+    acc8(s0, wa, c);
+    acc8(s1, wb, c);
+  }
+  s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, 4);
+  s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, 4);
+  s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, 2);
+  s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, 2);
+  s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, 1);
+  s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, 1);
+  sa = s0;
+  sb = s1;
+}
+
+// Split-precision rerank of keys[0..n) in place (approximate bfloat16
+// scores): eight rows per warp at a time, two per 8-lane group; a slot past n
+// re-reads the last candidate's row (the result is dropped).
 template <typename RowPtr>
 CEOS_DEV void rerank_bf16_inplace(uint64_t* keys, int n, const float* qv, int ldx, RowPtr row) {
   const int lane = threadIdx.x & 31;
@@ -138,12 +204,19 @@ CEOS_DEV void rerank_bf16_inplace(uint64_t* keys, int n, const float* qv, int ld
   const int warp = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   const int n8 = ldx >> 3;
-  for (int base = warp * 4; base < n; base += nw * 4) {
-    const int i = base + grp;
-    const bool active = i < n;
-    const int id = active ? key_id(keys[i]) : 0;
-    const float d = dot_g8_bf16(qv, active ? row(id) : nullptr, n8, g, active);
-    if (active && g == 0) keys[i] = pack_key(d, id);
+  const bool pf = n >= kRerankPrefetchMin;
+  for (int base = warp * 8; base < n; base += nw * 8) {
+    if (pf) prefetch_rows(keys, n, base + nw * 8, ldx * 2, row);
+    const int i0 = base + grp, i1 = base + 4 + grp;
+    const bool a0 = i0 < n, a1 = i1 < n;
+    const int id0 = key_id(keys[a0 ? i0 : n - 1]);
+    const int id1 = key_id(keys[a1 ? i1 : n - 1]);
+    float d0, d1;
+    dot_g8_bf16_2(qv, row(id0), row(id1), n8, g, d0, d1);
+    if (g == 0) {
+      if (a0) keys[i0] = pack_key(d0, id0);
+      if (a1) keys[i1] = pack_key(d1, id1);
+    }
   }
 }
 
@@ -210,7 +283,9 @@ CEOS_DEV void rerank_inplace(uint64_t* keys, int n, const float* qv, int ldx, Ro
   const int warp = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5;
   const int n4 = ldx >> 2;
+  const bool pf = n >= kRerankPrefetchMin;
   for (int base = warp * 8; base < n; base += nw * 8) {
+    if (pf) prefetch_rows(keys, n, base + nw * 8, ldx * 4, row);
     const int i0 = base + grp, i1 = base + 4 + grp;
     const bool a0 = i0 < n, a1 = i1 < n;
     const int id0 = key_id(keys[a0 ? i0 : n - 1]);
@@ -730,8 +805,10 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
   const int k_cap = np2(a.k > 0 ? a.k : 1);
   const int npts = (int)a.n_points;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int2* bufA = a.sort_scratch + (long)blockIdx.x * 2 * a.sort_cap;
-  int2* bufB = bufA + a.sort_cap;
+  // the first scatter pass writes bufA: the buffers of all CTAs' first passes
+  // (the only pass of the partitioned accumulation) form one contiguous range
+  int2* bufA = a.sort_scratch + (long)blockIdx.x * a.sort_cap;
+  int2* bufB = a.sort_scratch + ((long)gridDim.x + blockIdx.x) * a.sort_cap;
 
   const int nq = a.d_nq ? min(*a.d_nq, a.nq) : a.nq;
   for (int q = blockIdx.x; q < nq; q += gridDim.x) {
@@ -804,8 +881,8 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     }
     __syncthreads();
     // ---- 3. stable scatter(s) by id digits ----
-    int2* src = bufA;
-    int2* dst = bufB;
+    int2* src = bufB;
+    int2* dst = bufA;
     const int w0 = min(E, warp * seg), w1 = min(E, w0 + seg);
     int* pstart = reinterpret_cast<int*>(sm + Lq.rhist + kPartStartOff);
     const int npass = part ? 1 : (a.id_bits + 7) / 8;
