@@ -64,6 +64,7 @@ SIGNATURES = {
     "ceos_device_count": (C.c_int, []),
     "ceos_set_log_level": (None, [C.c_int]),
     "ceos_flush_l2": (C.c_int, [C.c_long]),
+    "ceos_debug_stall_tensor_products": (C.c_int, [C.c_int]),
     "ceos_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(VP)]),
     "ceos_destroy": (None, [VP]),
     "ceos_set_index_param": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),

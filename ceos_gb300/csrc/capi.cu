@@ -21,6 +21,11 @@ int ceos_device_count(void) {
 }
 void ceos_set_log_level(int level) { g_log = level < 0 ? 0 : level; }
 
+int ceos_debug_stall_tensor_products(int polls) {
+  project_t5_set_stall(polls < 0 ? 0 : polls);
+  return CEOS_OK;
+}
+
 int ceos_flush_l2(long bytes) {
   static DevBuf* flush = nullptr;
   if (bytes <= 0) return fail(CEOS_ERR_ARG, "bytes must be > 0");

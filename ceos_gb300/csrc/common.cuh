@@ -257,7 +257,16 @@ constexpr int kBinSortMax = 24;
 template <bool kBinOrder = false, int kLoadsU = kTopkU, typename GetItem>
 __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32_t* hist,
                                uint64_t* maybe, int maybe_cap, uint32_t* scratch,
-                               const uint32_t* pre = nullptr) {
+                               const uint32_t* pre = nullptr, const int2* pf_items = nullptr) {
+  // pf_items: the items as 8-byte records in global memory, when get() reads
+  // them there; each round of loads then prefetches the next round into L2,
+  // one 128-byte line (16 items) per thread
+  auto pf_round = [&](long next) {
+    if (pf_items == nullptr) return;
+    const long i = next + 16L * threadIdx.x;
+    if (16 * threadIdx.x < kLoadsU * blockDim.x && i < N)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(pf_items + i));
+  };
   const int lane = threadIdx.x & 31;
   if (kBinOrder && threadIdx.x == 0) {
     scratch[12] = 0u;
@@ -353,6 +362,7 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) hist[b] = 0;
   __syncthreads();
   for (long base = 0; base < N; base += kLoadsU * blockDim.x) {
+    pf_round(base + kLoadsU * blockDim.x);
     float v[kLoadsU];
     int id[kLoadsU];
     bool ok[kLoadsU];
@@ -411,6 +421,7 @@ __device__ int block_topk_hist(GetItem get, long N, int K, uint64_t* out, uint32
   const bool fits = inbin <= (uint32_t)maybe_cap;
   // ---- pass 3: compaction ----
   for (long base = 0; base < N; base += kLoadsU * blockDim.x) {
+    pf_round(base + kLoadsU * blockDim.x);
     float v[kLoadsU];
     int id[kLoadsU];
     bool ok[kLoadsU];

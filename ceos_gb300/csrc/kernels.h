@@ -45,6 +45,9 @@ cudaError_t launch_project_tc(const ProjArgs& a, int mode, int L, int num_sms, c
 // synchronizing the stream.
 cudaError_t launch_project_t5(const ProjArgs& a, int mode, cudaStream_t st, int num_sms);
 int project_t5_take_faults(cudaStream_t st);
+// test hook: polls > 0 makes the following launches issue no products and
+// give up each wait after `polls` polls (0: normal operation)
+void project_t5_set_stall(int polls);
 
 // ---- selection (select.cu) ----
 // Per column of the row-major sample samp[S][C]: u32 key thresholds, the lower

@@ -86,6 +86,7 @@ constexpr int kWaitPolls = 1 << 24;
 constexpr uint32_t kWaitHintNs = 20000;  // the fault path's waits: suspend hint
 
 __device__ unsigned g_t5_faults = 0;
+int g_t5_stall_polls = 0;  // test hook (project_t5_set_stall)
 
 CEOS_DEV uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -136,8 +137,11 @@ CEOS_DEV uint32_t bf16x2(float lo, float hi) {
 
 // 17 warps: five of them share one of the SM's four 16,384-register
 // partitions, so a thread has at most 96 registers.
-template <int MODE>
-__global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
+// kStall (test hook, a separate instantiation so that the products' path is
+// compiled without it): no products are issued, and every wait gives up
+// after stall_polls polls.
+template <int MODE, bool kStall>
+__global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a, int stall_polls) {
   extern __shared__ __align__(1024) unsigned char sm[];
   const int t = threadIdx.x, w = t >> 5, l = t & 31;
   const bool mma_warp = w == kT5Threads / 32;  // the last warp issues the products
@@ -198,8 +202,9 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
   // a bounded wait that also gives up once the other side has faulted (no
   // suspend hint: a product takes about a microsecond, and a suspended warp
   // wakes later than a polling one)
+  const int wait_polls = kStall ? stall_polls : kWaitPolls;
   auto wait = [&](uint64_t* b, uint32_t parity) -> bool {
-    for (int it = 0; it < kWaitPolls; ++it) {
+    for (int it = 0; it < wait_polls; ++it) {
       uint32_t ok;
       asm volatile(
           "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
     int issued[kSlots];  // commits per slot
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) issued[s] = 0;
-    bool ok = true;
+    bool ok = !kStall;
     for (long t0 = (long)kSlots * blockIdx.x; t0 < n_tiles && ok; t0 += (long)kSlots * gridDim.x) {
       for (int st = 0; st < steps && ok; ++st) {
 #pragma unroll
@@ -544,13 +549,15 @@ __global__ void __launch_bounds__(kT5Threads + 32, 1) k_project_t5(ProjArgs a) {
 
 template <int MODE>
 static cudaError_t launch_t5(const ProjArgs& a, int num_sms, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_project_t5<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+  const bool stall = g_t5_stall_polls > 0;
+  auto kern = stall ? k_project_t5<MODE, true> : k_project_t5<MODE, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
   if (e != cudaSuccess) return e;
   const long groups = (a.n_rows + kSlots * kT5Vec - 1) / (kSlots * kT5Vec);
   long blocks = num_sms;  // one CTA per SM (shared memory and tensor memory)
   if (blocks > groups) blocks = groups;
   if (blocks < 1) blocks = 1;
-  k_project_t5<MODE><<<(unsigned)blocks, kT5Threads + 32, kSmem, st>>>(a);
+  kern<<<(unsigned)blocks, kT5Threads + 32, kSmem, st>>>(a, g_t5_stall_polls);
   return cudaGetLastError();
 }
 
@@ -563,6 +570,8 @@ cudaError_t launch_project_t5(const ProjArgs& a, int mode, cudaStream_t st, int 
   }
   return cudaErrorInvalidValue;
 }
+
+void project_t5_set_stall(int polls) { g_t5_stall_polls = polls; }
 
 int project_t5_take_faults(cudaStream_t st) {
   unsigned h = 0, zero = 0;

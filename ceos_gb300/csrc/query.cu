@@ -1184,8 +1184,10 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
       v = __int_as_float(w.y);
       return w.x >= 0;
     };
-    // eight items in flight per thread: the sums come from L2 or HBM
-    const int nc = block_topk_hist<false, 8>(sget, (long)(part ? E : U), a.c, cand, hist, maybe, kMaybe, scratch, pre);
+    // eight items in flight per thread, and the next round prefetched: the
+    // sums come from L2 or HBM
+    const int nc = block_topk_hist<false, 8>(sget, (long)(part ? E : U), a.c, cand, hist, maybe, kMaybe, scratch,
+                                             pre, sums);
     const int ns2 = score_candidates(a, rq, cand, nc, qv, resc, hist, maybe, kMaybe, scratch);
     const int nres = block_topk_hist_sorted(
         [&](long i, float& v, int& id) {

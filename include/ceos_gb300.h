@@ -71,6 +71,13 @@ void ceos_set_log_level(int level);
  * call starts with a cold L2; synchronizes the device. */
 int ceos_flush_l2(long bytes);
 
+/* Test hook (no reference counterpart): with polls > 0, the tcgen05 projections that follow
+ * (split precision, fhtDim 1024) issue no tensor-core products and give up every wait after
+ * `polls` polls, so a test can check that a projection whose products never complete ends
+ * its blocks, frees their tensor memory and is reported as CEOS_ERR_CUDA by the build, with
+ * the device still usable. polls = 0 restores normal operation. Returns 0. */
+int ceos_debug_stall_tensor_products(int polls);
+
 /* ---- CEOs (src/CEOs.h:18-114) ----------------------------------------- */
 /* CEOs(n_points, n_features): python/python_wrapper.cpp:14-21, src/CEOs.h:58-61 */
 int ceos_create(int n_points, int n_features, ceos_index** out);

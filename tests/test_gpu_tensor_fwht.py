@@ -99,3 +99,33 @@ def test_tensor_sampled_build_selects_exactly(gpu, d, D, R):
             top = cand[np.lexsort((cand, -key[cand]))][:m]
             assert np.array_equal(bi[col, end], top), (col, end)
             assert np.array_equal(bv[col, end].view(np.uint32), vals[top].view(np.uint32)), (col, end)
+
+
+def test_tensor_projection_stall_is_reported(gpu):
+    """A tcgen05 projection whose products never complete (test hook: no
+    products are issued and every wait gives up after 64 polls) ends its
+    blocks and frees their tensor memory; the build reports CEOS_ERR_CUDA, and
+    the device stays usable: the same build then succeeds and searches."""
+    from ceos_gb300 import _capi
+
+    n, d = 20000, 960
+    X = gist_like(n, d, seed=31)
+    L = _capi.lib()
+    g = gpu.CEOs(n, d)
+    g.setIndexParam(1024, 1, 50, 1, 42)
+    g.precision = "split_bf16"
+    assert L.ceos_debug_stall_tensor_products(64) == 0
+    try:
+        with pytest.raises(_capi.CEOsError, match="did not complete"):
+            g.build_coCEOs_Est(X)
+    finally:
+        L.ceos_debug_stall_tensor_products(0)
+    h = gpu.CEOs(n, d)
+    h.setIndexParam(1024, 1, 50, 1, 42)
+    h.precision = "split_bf16"
+    h.build_coCEOs_Est(X)
+    h.n_probed_vectors, h.n_cand = 10, 200
+    ids, dists = h.search_coCEOs_Est(X[:16], 5)
+    assert ids.shape == (16, 5) and np.all((ids >= 0) & (ids < n))
+    exact = np.einsum("qkd,qd->qk", X[ids].astype(np.float64), X[:16].astype(np.float64))
+    assert np.max(np.abs(dists - exact) / np.abs(exact)) < 1e-5
