@@ -851,7 +851,7 @@ extern "C" int ceos_search_coceos_est_device_noalloc(ceos_index* h, const float*
   // Every buffer above is fully written before it is read (the hash tables
   // are reset per query inside the kernel), so no clearing is needed.
   CUDA_TRY(launch_pad_rows(d_Q, nq, c.n_features, qpad, c.ldx, st));
-  ProjArgs a = c.proj_base();
+  ProjArgs a = c.query_proj_base();
   a.X = qpad;
   a.head = 0;
   a.cap_rows = LONG_MAX;

@@ -205,8 +205,9 @@ struct Core {
   int reserve = -1;
   DevBuf dCnt, dTau;
   // transform of the built index: 1 = split-precision tensor-core FWHT, taken
-  // from the precision at build time and used for every later projection
-  // (queries, updates) so that query and bucket projections agree
+  // from the precision at build time and used for every later projection of
+  // index rows (updates, refills), so that all bucket values come from one
+  // transform; query projections use the FP32 kernel (query_proj_base)
   int proj_tensor = 0;
 
   int C() const { return n_proj * n_repeats; }
@@ -320,6 +321,17 @@ struct Core {
     a.R = n_repeats;
     a.signs = dSigns.as<uint32_t>();
     a.tensor = proj_tensor;
+    return a;
+  }
+
+  // Query projections run on the FP32 kernel in either precision: a batch of
+  // queries is too few rows for the tensor-core tiles (16 rows each, two per
+  // SM) to fill the GPU, so the FP32 butterflies are faster there, and every
+  // query's projection is the same whatever its batch. Only the probe choice
+  // reads them; the buckets keep the index's precision.
+  ProjArgs query_proj_base() const {
+    ProjArgs a = proj_base();
+    a.tensor = 0;
     return a;
   }
 
@@ -493,7 +505,7 @@ struct Core {
     }
     timer.mark("h2d+stage");
     CUDA_TRY(wQproj.ensure((size_t)nq * C() * 4));
-    ProjArgs a = proj_base();
+    ProjArgs a = query_proj_base();
     a.X = wQ.as<float>();
     a.head = 0;
     a.cap_rows = LONG_MAX;

@@ -201,7 +201,7 @@ struct ceos_server {
       CUDA_TRY(cudaMemcpyAsync(sl.dStage.p, sl.hQ.p, raw, cudaMemcpyHostToDevice, st));
       CUDA_TRY(launch_pad_rows(sl.dStage.as<float>(), rows, d, sl.dQ.as<float>(), ldx, st));
     }
-    ProjArgs a = core->proj_base();
+    ProjArgs a = core->query_proj_base();
     a.X = sl.dQ.as<float>();
     a.head = 0;
     a.cap_rows = LONG_MAX;
