@@ -107,7 +107,9 @@ int ceos_set_centering(ceos_index* h, int centering);
 int ceos_get_centering(const ceos_index* h, int* centering);
 /* CEOS_PRECISION_* for the next search (no counterpart in the reference). The split form
  * scans the candidates' rows in bfloat16 (a copy made on the first split search) and
- * rescores the best 4 * n_neighbors of that scan exactly in FP32. */
+ * rescores the best 4 * n_neighbors of that scan exactly in FP32. Set before a build, it
+ * also makes that build and the index's later updates project on the tensor cores (split
+ * bfloat16 FWHT, fhtDim 256 and 1024); query projections use the FP32 transform either way. */
 int ceos_set_precision(ceos_index* h, int precision);
 
 /* build(dataset): python/python_wrapper.cpp:39 -> CEOs::build_CEOs, src/CEOs.cpp:18-98.
