@@ -568,6 +568,12 @@ struct Core {
       const int grid = (int)std::min<long>(nq, (long)sms * std::max(query_sorted_blocks_per_sm(ssm), 1));
       CUDA_TRY(wSort.ensure((size_t)std::max(grid, 1) * 2 * q.sort_cap * 8));
       q.sort_scratch = wSort.as<int2>();
+      // the probes of every query, chosen by a kernel of their own (many small
+      // blocks hide the selection's latency better than the query CTAs)
+      CUDA_TRY(wProbes.ensure((size_t)nq * std::max(s, 1) * 4));
+      q.probes_out = wProbes.as<int>();
+      CUDA_TRY(launch_probe_select(q, stream));
+      q.probes = wProbes.as<int>();
       CUDA_TRY(launch_query_sorted(q, std::max(grid, 1), ssm, stream));
       return finish_search(mode, nq, k, ids, dists, out_ids, out_d, on_device);
     }

@@ -818,17 +818,25 @@ __global__ void __launch_bounds__(kQueryThreads, MINB) k_query_sorted(QueryArgs 
     const int rq = (a.q_k && a.rescore_per_k > 0) ? min(a.rescore, a.rescore_per_k * kq) : a.rescore;
     for (int j = threadIdx.x; j < a.ldx; j += blockDim.x) qv[j] = a.Q[(long)q * a.ldx + j];
     // ---- 1. probes: top-s |projection|, consumed worst first ----
-    const float* qp = a.qproj + (long)q * a.C;
-    const int ns = block_topk_hist_sorted(
-        [&](long i, float& v, int& id) {
-          v = abs_ref(qp[i]);
-          id = (int)i;
-          return true;
-        },
-        (long)a.C, sq, pkeys, s_cap, hist, maybe, kMaybe, scratch);
-    for (int j = threadIdx.x; j < ns; j += blockDim.x) {
-      const int col = key_id(pkeys[ns - 1 - j]);
-      probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
+    // (taken from a.probes when k_probe_select chose them for every query of
+    // the launch beforehand: same selection, same order)
+    int ns;
+    if (a.probes != nullptr && a.q_s == nullptr) {
+      ns = a.s;
+      for (int j = threadIdx.x; j < ns; j += blockDim.x) probes[j] = a.probes[(long)q * a.s + j];
+    } else {
+      const float* qp = a.qproj + (long)q * a.C;
+      ns = block_topk_hist_sorted(
+          [&](long i, float& v, int& id) {
+            v = abs_ref(qp[i]);
+            id = (int)i;
+            return true;
+          },
+          (long)a.C, sq, pkeys, s_cap, hist, maybe, kMaybe, scratch);
+      for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+        const int col = key_id(pkeys[ns - 1 - j]);
+        probes[j] = qp[col] < 0 ? -(col + 1) : (col + 1);
+      }
     }
     __syncthreads();
     // ---- 2. digit counts of the probed pairs ----
