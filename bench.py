@@ -934,7 +934,9 @@ def main():
             "parity": parity,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": Q.nbytes,
                     "d2h_bytes_per_step": nq * k * 8},
-            "gpu_launches": 3 * args.steps,
+            # per step: k_pad_rows (queries padded to ldx), k_project (query
+            # projections), k_probe_select, k_query_sorted
+            "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }
     rt.free(dQ)
